@@ -1,0 +1,703 @@
+// S(Q,omega) job pipeline: the frame loop of mp_sqom (code/src/mp_sqom56.f90:965-1165) on the
+// GPU.  Per frame, one kernel selects atoms, computes their NUFFT phases and strengths and
+// bins them (mp_sqom56.f90:1100-1143 fused into the binning), one kernel spreads all species
+// grids, cuFFT transforms them, and one kernel deconvolves, separates packed species pairs,
+// applies the species weights (:1338-1377, weight tables :901-936) and stores the weighted
+// amplitude cs(t,Q) of the frame.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mpsq_internal.h"
+
+namespace mpsq {
+
+// Parameters of the per-point preparation, passed by value.
+struct PrepArgs {
+  int dim;
+  int n_species;
+  int64_t species_offset[MPSQ_MAX_SPECIES + 1];
+  int group_of[MPSQ_MAX_SPECIES];  // -1: species not transformed (mask 0)
+  int comp_of[MPSQ_MAX_SPECIES];   // 0 real / 1 imaginary component in a packed pair
+  int input_method;
+  int phase_rounding;
+  int use_range;
+  int bulk_nsuper1;
+  int n_row[3];
+  double axis[3][3];
+  float axis_f[3][3];
+  double tpe[3];
+  float tpe_f[3];
+  double centre[3];
+  float centre_f[3];
+  double pos_min[3], pos_max[3];
+  float pos_min_f[3], pos_max_f[3];
+  float tol_f;
+  int has_qc;
+  double q_center[3];
+  float tpq_f[3];  // 2 pi q_center in FP32 (reference rounding)
+  int window;
+  int pack;
+  int64_t n_atoms_frame;
+};
+
+// Parameters of the fused deconvolution / weighting.
+struct WeightArgs {
+  int ngroups;
+  int pair[MPSQ_MAX_SPECIES];      // per group: 1 if it holds two species
+  int sp_a[MPSQ_MAX_SPECIES];      // species in the real component (or the only one)
+  int sp_b[MPSQ_MAX_SPECIES];      // species in the imaginary component
+  int weight_mode;
+  double b_coh[MPSQ_MAX_SPECIES];  // evaluated in the job's precision
+  double xff[MPSQ_MAX_SPECIES][9];
+  double kappa;                     // |Q|^2 -> exponent scale of the form factor
+  double q0[3];
+  double qs[3][3];
+  double extra_sq;
+  double wnorm;
+  int store_species;
+  int n_species;
+};
+
+}  // namespace mpsq
+
+using namespace mpsq;
+
+struct mpsq_job {
+  mpsq_job_desc d{};
+  cudaStream_t s = nullptr;
+  EsKernel es{};
+  GridGeom g{};
+  SpreadArgs sa{};
+  PrepArgs pa{};
+  WeightArgs wa{};
+  int ngroups = 0;
+  float4* traj = nullptr;
+  int4* at_ind = nullptr;
+  void* fine = nullptr;
+  int* counts = nullptr;
+  int* starts = nullptr;
+  void* recs = nullptr;
+  void* str = nullptr;
+  int64_t cap = 0;
+  void* corr[3] = {nullptr, nullptr, nullptr};
+  void* cs = nullptr;
+  void* cs_species = nullptr;
+  cufftHandle fft = 0;
+  bool have_fft = false;
+  int* err = nullptr;
+  bool profile = false;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double stage_ms[4] = {0, 0, 0, 0};
+  int64_t stage_frames = 0;
+};
+
+namespace mpsq {
+
+__device__ __forceinline__ double to_grid_j(double x, double nf) {
+  double g = x * (nf * 0.15915494309189533576888376337251436);
+  g -= nf * floor(g / nf);
+  if (g >= nf) g -= nf;
+  if (!(g >= 0.0 && g < nf)) g = 0.0;  // NaN / inf coordinates: keep every index in range
+  return g;
+}
+
+// Same halo-copy emission as the plan API (kept local to this unit so it inlines).
+template <typename T>
+__device__ __forceinline__ void emit_job(const SpreadArgs& a, const double g[3], int keygrid,
+                                         int comp, bool scatter, int* cursor,
+                                         const int* starts, typename RecOf<T>::type* recs,
+                                         typename Cplx<T>::type* str_out,
+                                         typename Cplx<T>::type strength, int64_t cap,
+                                         int* err) {
+  int64_t i0[3], tlo[3], thi[3];
+  T d[3];
+  for (int k = 0; k < 3; ++k) {
+    if (k < a.dim) {
+      const int64_t s = (int64_t)ceil(g[k] - 0.5 * a.w);
+      i0[k] = s;
+      d[k] = (T)((double)s - g[k]);
+      tlo[k] = s >= 0 ? s / a.tile[k] : -((-s + a.tile[k] - 1) / a.tile[k]);
+      const int64_t e = s + a.w - 1;
+      thi[k] = e >= 0 ? e / a.tile[k] : -((-e + a.tile[k] - 1) / a.tile[k]);
+    } else {
+      i0[k] = 0;
+      d[k] = (T)0;
+      tlo[k] = thi[k] = 0;
+    }
+  }
+  for (int64_t tz = tlo[2]; tz <= thi[2]; ++tz) {
+    const int64_t wz = ((tz % a.ntile[2]) + a.ntile[2]) % a.ntile[2];
+    const int lz = (int)(i0[2] - tz * a.tile[2]);
+    for (int64_t ty = tlo[1]; ty <= thi[1]; ++ty) {
+      const int64_t wy = ((ty % a.ntile[1]) + a.ntile[1]) % a.ntile[1];
+      const int ly = (int)(i0[1] - ty * a.tile[1]);
+      for (int64_t tx = tlo[0]; tx <= thi[0]; ++tx) {
+        const int64_t wx = ((tx % a.ntile[0]) + a.ntile[0]) % a.ntile[0];
+        const int lx = (int)(i0[0] - tx * a.tile[0]);
+        const int64_t key = (int64_t)keygrid * a.n_tiles + (wz * a.ntile[1] + wy) * a.ntile[0] + wx;
+        const int slot = atomicAdd(&cursor[key], 1);
+        if (!scatter) continue;
+        const int64_t pos = (int64_t)starts[key] + slot;
+        if (pos >= (int64_t)starts[key + 1] || pos >= cap) {
+          atomicOr(err, kErrRecOverflow);
+          continue;
+        }
+        typename RecOf<T>::type r;
+        r.dx = d[0];
+        r.dy = d[1];
+        r.dz = d[2];
+        r.packed = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
+        recs[pos] = r;
+        str_out[pos] = strength;
+      }
+    }
+  }
+}
+
+// Selection, phases and strengths of one atom of one frame (mp_sqom56.f90:1104-1142), then
+// binning.  Pass 0 counts, pass 1 scatters.
+template <typename T>
+__global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
+                               PrepArgs p, SpreadArgs a, int scatter, int* cursor,
+                               const int* __restrict__ starts, typename RecOf<T>::type* recs,
+                               typename Cplx<T>::type* str, int64_t cap, int* err) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.n_atoms_frame) return;
+  int s = 0;
+  while (s + 1 < p.n_species && j >= p.species_offset[s + 1]) ++s;
+  if (j < p.species_offset[0] || j >= p.species_offset[p.n_species]) return;
+  const int grid = p.group_of[s];
+  if (grid < 0) return;
+  const float4 r = frame[j];
+  if (p.input_method == MPSQ_CELL) {
+    if (r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) return;  // vacancy (:1107)
+    if (p.use_range && at_ind) {
+      const int4 ci = at_ind[j];
+      const int c3[3] = {ci.x, ci.y, ci.z};
+      for (int k = 0; k < 3; ++k) {
+        const int c = c3[k] - p.n_row[k] / 2 - 1;
+        if ((double)c < p.pos_min[k] || (double)c > p.pos_max[k]) return;  // (:1109-1111)
+      }
+    }
+  } else {
+    const float rr[3] = {r.x, r.y, r.z};
+    for (int k = 0; k < 3; ++k)  // (:1121-1128)
+      if (!(rr[k] >= p.pos_min_f[k] - p.tol_f && rr[k] < p.pos_max_f[k] + p.tol_f)) return;
+  }
+  double x[3] = {0.0, 0.0, 0.0};
+  double g[3] = {0.0, 0.0, 0.0};
+  const double rd[3] = {(double)r.x, (double)r.y, (double)r.z};
+  const float rf[3] = {r.x, r.y, r.z};
+  for (int k = 0; k < p.dim; ++k) {
+    if (p.phase_rounding) {
+      // FP32 dot product and FP32 scale as the reference computes xf, yf (:1115-1116)
+      float pr = 0.0f;
+      for (int b = 0; b < 3; ++b) pr = __fadd_rn(pr, __fmul_rn(p.axis_f[k][b], __fsub_rn(rf[b], p.centre_f[b])));
+      x[k] = (double)__fmul_rn(pr, p.tpe_f[k]);
+    } else {
+      double pr = 0.0;
+      for (int b = 0; b < 3; ++b) pr += p.axis[k][b] * (rd[b] - p.centre[b]);
+      x[k] = pr * p.tpe[k];
+    }
+    g[k] = to_grid_j(x[k], (double)a.nf[k]);
+  }
+  typename Cplx<T>::type c;
+  if (p.has_qc) {
+    if (p.phase_rounding) {
+      float arg = 0.0f;
+      for (int b = 0; b < 3; ++b) arg = __fadd_rn(arg, __fmul_rn(p.tpq_f[b], rf[b]));
+      // the argument carries the reference's FP32 rounding; the exponential itself is
+      // evaluated in the job's precision
+      if (sizeof(T) == 8) {
+        double sn, cn;
+        sincos((double)arg, &sn, &cn);
+        c.x = (T)cn;
+        c.y = (T)(-sn);
+      } else {
+        float sn, cn;
+        sincosf(arg, &sn, &cn);
+        c.x = (T)cn;
+        c.y = (T)(-sn);
+      }
+    } else {
+      double turns = 0.0;
+      for (int b = 0; b < 3; ++b) turns += p.q_center[b] * rd[b];
+      turns -= floor(turns);
+      if (sizeof(T) == 8) {
+        double sn, cn;
+        sincospi(2.0 * turns, &sn, &cn);
+        c.x = (T)cn;
+        c.y = (T)(-sn);
+      } else {
+        float sn, cn;
+        sincospif((float)(2.0 * turns), &sn, &cn);
+        c.x = (T)cn;
+        c.y = (T)(-sn);
+      }
+    }
+  } else {
+    c.x = (T)1;
+    c.y = (T)0;
+  }
+  if (p.window) {  // spatial Hann window (1+cos x)(1+cos y) (:1118)
+    const int nw = p.dim == 2 ? 2 : 3;
+    T f = (T)1;
+    for (int k = 0; k < nw; ++k) f *= (T)1 + (T)cos(x[k]);
+    c.x *= f;
+    c.y *= f;
+  }
+  const int comp = p.pack ? p.comp_of[s] : 0;
+  if (p.pack && c.x == (T)0) return;  // zero strength contributes nothing
+  emit_job<T>(a, g, grid, comp, scatter != 0, cursor, starts, recs, str, c, cap, err);
+}
+
+template <typename T>
+__device__ __forceinline__ T species_weight(const WeightArgs& w, int s, T s2) {
+  if (w.weight_mode == MPSQ_WEIGHT_NEUTRON) return (T)w.b_coh[s];
+  if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+    T f = (T)w.xff[s][8];
+    for (int i = 0; i < 4; ++i) f += (T)w.xff[s][2 * i] * exp(-(T)w.xff[s][2 * i + 1] * s2);
+    return f;
+  }
+  return (T)1;
+}
+
+// Deconvolution, pair separation, species weighting; writes cs(t, Q) for one frame.
+template <typename T>
+__global__ void job_deconv_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t m2,
+                                  const typename Cplx<T>::type* __restrict__ fine,
+                                  const T* __restrict__ c0, const T* __restrict__ c1,
+                                  const T* __restrict__ c2, WeightArgs w,
+                                  typename Cplx<T>::type* __restrict__ cs_frame,
+                                  typename Cplx<T>::type* __restrict__ cs_species_frame) {
+  using C = typename Cplx<T>::type;
+  const int64_t nm = m0 * m1 * m2;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nm) return;
+  const int64_t i = q % m0, j = (q / m0) % m1, l = q / (m0 * m1);
+  const int64_t kx = i - m0 / 2, ky = j - m1 / 2, kz = l - m2 / 2;
+  const int64_t nf0 = a.nf[0], nf1 = a.nf[1], nf2 = a.nf[2];
+  const int64_t src = (((kz + nf2) % nf2) * nf1 + ((ky + nf1) % nf1)) * nf0 + ((kx + nf0) % nf0);
+  const int64_t srcm = (((nf2 - kz) % nf2) * nf1 + ((nf1 - ky) % nf1)) * nf0 + ((nf0 - kx) % nf0);
+  const T corr = c0[i] * c1[j] * c2[l];
+  T s2 = 0;
+  if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+    T qv[3];
+    for (int b = 0; b < 3; ++b)
+      qv[b] = (T)w.q0[b] + (T)kx * (T)w.qs[0][b] + (T)ky * (T)w.qs[1][b] + (T)kz * (T)w.qs[2][b];
+    s2 = (T)w.kappa * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + (T)w.extra_sq);
+  }
+  T accr = 0, acci = 0;
+  for (int gi = 0; gi < w.ngroups; ++gi) {
+    const C G = fine[gi * a.n_fine + src];
+    if (w.pair[gi]) {
+      const C Gm = fine[gi * a.n_fine + srcm];
+      const T ar = (T)0.5 * (G.x + Gm.x) * corr, ai = (T)0.5 * (G.y - Gm.y) * corr;
+      const T br = (T)0.5 * (G.y + Gm.y) * corr, bi = (T)(-0.5) * (G.x - Gm.x) * corr;
+      const int sa = w.sp_a[gi], sb = w.sp_b[gi];
+      const T wa = species_weight<T>(w, sa, s2), wb = species_weight<T>(w, sb, s2);
+      accr += wa * ar + wb * br;
+      acci += wa * ai + wb * bi;
+      if (w.store_species) {
+        C va, vb;
+        va.x = ar * (T)w.wnorm;
+        va.y = ai * (T)w.wnorm;
+        vb.x = br * (T)w.wnorm;
+        vb.y = bi * (T)w.wnorm;
+        cs_species_frame[(int64_t)sa * nm + q] = va;
+        cs_species_frame[(int64_t)sb * nm + q] = vb;
+      }
+    } else {
+      const int sa = w.sp_a[gi];
+      const T wa = species_weight<T>(w, sa, s2);
+      accr += wa * G.x * corr;
+      acci += wa * G.y * corr;
+      if (w.store_species) {
+        C va;
+        va.x = G.x * corr * (T)w.wnorm;
+        va.y = G.y * corr * (T)w.wnorm;
+        cs_species_frame[(int64_t)sa * nm + q] = va;
+      }
+    }
+  }
+  C out;
+  out.x = accr * (T)w.wnorm;
+  out.y = acci * (T)w.wnorm;
+  cs_frame[q] = out;
+}
+
+static size_t csize(int prec) { return prec == MPSQ_FP64 ? sizeof(double2) : sizeof(float2); }
+static size_t rsize(int prec) { return prec == MPSQ_FP64 ? sizeof(RecD) : sizeof(RecF); }
+
+static int job_layout(const mpsq_job_desc* d, EsKernel* es, GridGeom* g, int* ngroups,
+                      int group_of[], int comp_of[], int pair[], int sp_a[], int sp_b[],
+                      int* pack) {
+  if (d->ndim != 2 && d->ndim != 3) return fail(MPSQ_ERR_ARG, "job: ndim must be 2 or 3");
+  if (d->precision != MPSQ_FP32 && d->precision != MPSQ_FP64)
+    return fail(MPSQ_ERR_ARG, "job: bad precision");
+  if (d->n_species < 1 || d->n_species > MPSQ_MAX_SPECIES)
+    return fail(MPSQ_ERR_ARG, "job: n_species must be in 1..%d", MPSQ_MAX_SPECIES);
+  if (d->n_frames < 1) return fail(MPSQ_ERR_ARG, "job: n_frames must be >= 1");
+  if (d->n_atoms_frame < 1) return fail(MPSQ_ERR_ARG, "job: n_atoms_frame must be >= 1");
+  if (d->species_offset[0] < 0 || d->species_offset[d->n_species] > d->n_atoms_frame)
+    return fail(MPSQ_ERR_ARG, "job: species offsets outside the frame");
+  for (int s = 0; s < d->n_species; ++s)
+    if (d->species_offset[s + 1] < d->species_offset[s])
+      return fail(MPSQ_ERR_ARG, "job: species offsets not increasing");
+  if (d->weight_mode < 1 || d->weight_mode > 3) return fail(MPSQ_ERR_ARG, "job: bad weight_mode");
+  *es = es_params(d->eps, d->precision);
+  int rc = make_geom(d->ndim, d->n_modes, es->w, g);
+  if (rc) return rc;
+  const bool qc0 = d->q_center[0] == 0.0 && d->q_center[1] == 0.0 && d->q_center[2] == 0.0;
+  *pack = (qc0 && !d->no_pack) ? 1 : 0;
+  int n = 0;
+  int open = -1;  // group with a free imaginary slot
+  for (int s = 0; s < d->n_species; ++s) {
+    group_of[s] = -1;
+    comp_of[s] = 0;
+    if (!d->mask[s]) continue;
+    if (*pack && open >= 0) {
+      group_of[s] = open;
+      comp_of[s] = 1;
+      pair[open] = 1;
+      sp_b[open] = s;
+      open = -1;
+    } else {
+      group_of[s] = n;
+      pair[n] = 0;
+      sp_a[n] = s;
+      sp_b[n] = s;
+      if (*pack) open = n;
+      ++n;
+    }
+  }
+  *ngroups = n;
+  return MPSQ_OK;
+}
+
+}  // namespace mpsq
+
+// ================================================================================ C ABI
+static void job_free(mpsq_job* j) {
+  if (!j) return;
+  if (j->have_fft) cufftDestroy(j->fft);
+  cudaFree(j->traj);
+  cudaFree(j->at_ind);
+  cudaFree(j->fine);
+  cudaFree(j->counts);
+  cudaFree(j->starts);
+  cudaFree(j->recs);
+  cudaFree(j->str);
+  for (int a = 0; a < 3; ++a) cudaFree(j->corr[a]);
+  cudaFree(j->cs);
+  cudaFree(j->cs_species);
+  cudaFree(j->err);
+  for (auto& e : j->ev)
+    if (e) cudaEventDestroy(e);
+  delete j;
+}
+
+extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
+  if (!d || !bytes) return fail(MPSQ_ERR_ARG, "estimate: null pointer");
+  EsKernel es;
+  GridGeom g;
+  int ng, gof[MPSQ_MAX_SPECIES], cof[MPSQ_MAX_SPECIES], pr[MPSQ_MAX_SPECIES],
+      sa[MPSQ_MAX_SPECIES], sb[MPSQ_MAX_SPECIES], pack;
+  int rc = job_layout(d, &es, &g, &ng, gof, cof, pr, sa, sb, &pack);
+  if (rc) return rc;
+  const int64_t per = d->ndim == 3 ? 8 : 4;
+  int64_t b = 0;
+  b += (int64_t)d->n_frames * d->n_atoms_frame * 16;                  // trajectory
+  b += (int64_t)std::max(1, ng) * g.n_fine * (int64_t)csize(d->precision);  // fine grids
+  b += d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision));
+  b += (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8;
+  b += (int64_t)d->n_frames * g.n_modes * (int64_t)csize(d->precision);     // cs(t,Q)
+  if (d->store_species)
+    b += (int64_t)d->n_frames * d->n_species * g.n_modes * (int64_t)csize(d->precision);
+  b += g.n_fine * (int64_t)csize(d->precision) / 4;  // cuFFT work area (estimate)
+  *bytes = b;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** out) {
+  if (!d || !out) return fail(MPSQ_ERR_ARG, "job_create: null pointer");
+  *out = nullptr;
+  auto* j = new mpsq_job();
+  j->d = *d;
+  j->s = (cudaStream_t)stream;
+  int gof[MPSQ_MAX_SPECIES], cof[MPSQ_MAX_SPECIES], pr[MPSQ_MAX_SPECIES] = {0},
+      sa[MPSQ_MAX_SPECIES] = {0}, sb[MPSQ_MAX_SPECIES] = {0}, pack = 0;
+  int rc = job_layout(d, &j->es, &j->g, &j->ngroups, gof, cof, pr, sa, sb, &pack);
+  if (rc) {
+    delete j;
+    return rc;
+  }
+  const int prec = d->precision;
+  // spread geometry
+  SpreadArgs& a = j->sa;
+  a.dim = d->ndim;
+  a.w = j->es.w;
+  a.beta = j->es.beta;
+  for (int k = 0; k < 3; ++k) {
+    a.nf[k] = j->g.nf[k];
+    a.tile[k] = j->g.tile[k];
+    a.ntile[k] = j->g.ntile[k];
+  }
+  a.n_tiles = j->g.n_tiles;
+  a.n_fine = j->g.n_fine;
+  a.ngrid = std::max(1, j->ngroups);
+  // preparation parameters
+  PrepArgs& p = j->pa;
+  p.dim = d->ndim;
+  p.n_species = d->n_species;
+  for (int s = 0; s <= d->n_species; ++s) p.species_offset[s] = d->species_offset[s];
+  for (int s = 0; s < d->n_species; ++s) {
+    p.group_of[s] = gof[s];
+    p.comp_of[s] = cof[s];
+  }
+  p.input_method = d->input_method;
+  p.phase_rounding = d->phase_rounding;
+  p.use_range = d->use_range;
+  p.bulk_nsuper1 = d->bulk_nsuper1;
+  for (int k = 0; k < 3; ++k) {
+    p.n_row[k] = d->n_row[k];
+    for (int b = 0; b < 3; ++b) {
+      p.axis[k][b] = d->axis[k][b];
+      p.axis_f[k][b] = (float)d->axis[k][b];
+    }
+    p.tpe[k] = d->tpe[k];
+    p.tpe_f[k] = (float)d->tpe[k];
+    p.centre[k] = d->centre[k];
+    p.centre_f[k] = (float)d->centre[k];
+    p.pos_min[k] = d->pos_min[k];
+    p.pos_max[k] = d->pos_max[k];
+    p.pos_min_f[k] = (float)d->pos_min[k];
+    p.pos_max_f[k] = (float)d->pos_max[k];
+    p.q_center[k] = d->q_center[k];
+    p.tpq_f[k] = (float)(2.0 * M_PI) * (float)d->q_center[k];
+  }
+  p.tol_f = d->bulk_nsuper1 ? (float)d->eps_x : 1.0f;
+  p.has_qc = pack ? 0 : !(d->q_center[0] == 0.0 && d->q_center[1] == 0.0 && d->q_center[2] == 0.0);
+  p.window = d->spatial_window;
+  p.pack = pack;
+  p.n_atoms_frame = d->n_atoms_frame;
+  // weighting parameters
+  WeightArgs& w = j->wa;
+  w.ngroups = j->ngroups;
+  for (int gi = 0; gi < j->ngroups; ++gi) {
+    w.pair[gi] = pr[gi];
+    w.sp_a[gi] = sa[gi];
+    w.sp_b[gi] = sb[gi];
+  }
+  w.weight_mode = d->weight_mode;
+  for (int s = 0; s < d->n_species; ++s) {
+    w.b_coh[s] = d->b_coh[s];
+    for (int i = 0; i < 9; ++i) w.xff[s][i] = d->xff[s][i];
+  }
+  w.kappa = d->ff_convention == MPSQ_FF_STANDARD ? 1.0 / (16.0 * M_PI * M_PI) : 1.0 / 16.0;
+  for (int b = 0; b < 3; ++b) {
+    w.q0[b] = d->qphys_origin[b];
+    for (int k = 0; k < 3; ++k) w.qs[k][b] = d->qphys_step[k][b];
+  }
+  w.extra_sq = d->qphys_extra_sq;
+  w.wnorm = d->spatial_window ? (d->ndim == 2 ? 0.25 : 0.125) : 1.0;
+  w.store_species = d->store_species;
+  w.n_species = d->n_species;
+
+  // device memory
+  const int64_t per = d->ndim == 3 ? 8 : 4;
+  int64_t nsel = d->species_offset[d->n_species] - d->species_offset[0];
+  j->cap = std::max<int64_t>(1, nsel * per);
+  if (j->cap > (int64_t)INT32_MAX) {
+    job_free(j);
+    return fail(MPSQ_ERR_ARG, "job: too many atoms per frame for int32 bins");
+  }
+  const size_t cs = csize(prec);
+  const int64_t nkeys = (int64_t)a.ngrid * j->g.n_tiles;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** ptr, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(ptr, std::max<size_t>(bytes, 16));
+  };
+  A((void**)&j->traj, (size_t)d->n_frames * d->n_atoms_frame * sizeof(float4));
+  A(&j->fine, (size_t)a.ngrid * j->g.n_fine * cs);
+  A((void**)&j->counts, sizeof(int) * (nkeys + 1));
+  A((void**)&j->starts, sizeof(int) * (nkeys + 1));
+  A(&j->recs, (size_t)j->cap * rsize(prec));
+  A(&j->str, (size_t)j->cap * cs);
+  A(&j->cs, (size_t)d->n_frames * j->g.n_modes * cs);
+  if (d->store_species) A(&j->cs_species, (size_t)d->n_frames * d->n_species * j->g.n_modes * cs);
+  A((void**)&j->err, sizeof(int));
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    std::vector<double> c(j->g.m[k], 1.0);
+    if (k < d->ndim) es_correction(j->es, j->g.nf[k], j->g.m[k], c.data());
+    A(&j->corr[k], c.size() * (prec == MPSQ_FP64 ? 8 : 4));
+    if (e != cudaSuccess) break;
+    if (prec == MPSQ_FP64) {
+      e = cudaMemcpy(j->corr[k], c.data(), c.size() * 8, cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> cf(c.begin(), c.end());
+      e = cudaMemcpy(j->corr[k], cf.data(), c.size() * 4, cudaMemcpyHostToDevice);
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemset(j->err, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    job_free(j);
+    return fail(e == cudaErrorMemoryAllocation ? MPSQ_ERR_ALLOC : MPSQ_ERR_CUDA, "job_create: %s",
+                cudaGetErrorString(e));
+  }
+  rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
+  if (rc) {
+    job_free(j);
+    return rc;
+  }
+  j->have_fft = true;
+  *out = j;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_destroy(mpsq_job* j) {
+  if (j && j->s) cudaStreamSynchronize(j->s);
+  job_free(j);
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_set_frames(mpsq_job* j, const float* pos, int32_t first, int32_t count,
+                                   int host) {
+  if (!j || !pos) return fail(MPSQ_ERR_ARG, "set_frames: null pointer");
+  if (first < 0 || count < 0 || first + count > j->d.n_frames)
+    return fail(MPSQ_ERR_ARG, "set_frames: frames [%d, %d) outside [0, %d)", first, first + count,
+                j->d.n_frames);
+  const size_t bytes = (size_t)count * j->d.n_atoms_frame * sizeof(float4);
+  float4* dst = j->traj + (size_t)first * j->d.n_atoms_frame;
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(dst, pos, bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, j->s));
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_set_cell_index(mpsq_job* j, const int32_t* at_ind, int host) {
+  if (!j || !at_ind) return fail(MPSQ_ERR_ARG, "set_cell_index: null pointer");
+  if (!j->at_ind) MPSQ_CUDA_TRY(cudaMalloc(&j->at_ind, (size_t)j->d.n_atoms_frame * sizeof(int4)));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(j->at_ind, at_ind, (size_t)j->d.n_atoms_frame * sizeof(int4),
+                                host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, j->s));
+  return MPSQ_OK;
+}
+
+template <typename T>
+static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
+  using C = typename Cplx<T>::type;
+  using R = typename RecOf<T>::type;
+  cudaStream_t s = j->s;
+  const SpreadArgs& a = j->sa;
+  const int64_t nkeys = (int64_t)a.ngrid * a.n_tiles;
+  const int bt = 256;
+  const unsigned nb = (unsigned)((j->d.n_atoms_frame + bt - 1) / bt);
+  const int64_t nm = j->g.n_modes;
+  const bool prof = j->profile;
+  auto mark = [&](int k) -> int {
+    if (prof) MPSQ_CUDA_TRY(cudaEventRecord(j->ev[k], s));
+    return MPSQ_OK;
+  };
+  for (int32_t t = first; t < first + count; ++t) {
+    const float4* frame = j->traj + (size_t)t * j->d.n_atoms_frame;
+    if (mark(0)) return MPSQ_ERR_CUDA;
+    MPSQ_CUDA_TRY(cudaMemsetAsync(j->counts, 0, sizeof(int) * (nkeys + 1), s));
+    if (j->ngroups > 0) {
+      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 0, j->counts, j->starts,
+                                          (R*)j->recs, (C*)j->str, j->cap, j->err);
+      MPSQ_LAUNCH_CHECK();
+    }
+    int rc = launch_scan<T>(j->counts, j->starts, nkeys, s);
+    if (rc) return rc;
+    MPSQ_CUDA_TRY(cudaMemsetAsync(j->counts, 0, sizeof(int) * (nkeys + 1), s));
+    if (j->ngroups > 0) {
+      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 1, j->counts, j->starts,
+                                          (R*)j->recs, (C*)j->str, j->cap, j->err);
+      MPSQ_LAUNCH_CHECK();
+    }
+    if (mark(1)) return MPSQ_ERR_CUDA;
+    rc = launch_spread<T>(a, (const R*)j->recs, (const C*)j->str, j->starts, j->pa.pack != 0,
+                          (C*)j->fine, s);
+    if (rc) return rc;
+    if (mark(2)) return MPSQ_ERR_CUDA;
+    rc = exec_fft(j->fft, j->d.precision, j->fine, CUFFT_FORWARD);
+    if (rc) return rc;
+    if (mark(3)) return MPSQ_ERR_CUDA;
+    C* csf = (C*)j->cs + (size_t)t * nm;
+    C* css = j->cs_species ? (C*)j->cs_species + (size_t)t * j->d.n_species * nm : nullptr;
+    job_deconv_kernel<T><<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(
+        a, j->g.m[0], j->g.m[1], j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
+        (const T*)j->corr[1], (const T*)j->corr[2], j->wa, csf, css);
+    MPSQ_LAUNCH_CHECK();
+    if (prof) {
+      if (mark(4)) return MPSQ_ERR_CUDA;
+      MPSQ_CUDA_TRY(cudaEventSynchronize(j->ev[4]));
+      for (int k = 0; k < 4; ++k) {
+        float ms = 0.0f;
+        MPSQ_CUDA_TRY(cudaEventElapsedTime(&ms, j->ev[k], j->ev[k + 1]));
+        j->stage_ms[k] += ms;
+      }
+      j->stage_frames += 1;
+    }
+  }
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_transform(mpsq_job* j, int32_t first, int32_t count) {
+  if (!j) return fail(MPSQ_ERR_ARG, "transform: null job");
+  if (first < 0 || count < 0 || first + count > j->d.n_frames)
+    return fail(MPSQ_ERR_ARG, "transform: frames outside the trajectory");
+  return j->d.precision == MPSQ_FP64 ? job_transform_t<double>(j, first, count)
+                                     : job_transform_t<float>(j, first, count);
+}
+
+extern "C" int mpsq_job_profile(mpsq_job* j, int enable) {
+  if (!j) return fail(MPSQ_ERR_ARG, "profile: null job");
+  if (enable)
+    for (auto& e : j->ev)
+      if (!e) MPSQ_CUDA_TRY(cudaEventCreate(&e));
+  j->profile = enable != 0;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_stage_ms(mpsq_job* j, double* ms4, int64_t* frames, int reset) {
+  if (!j) return fail(MPSQ_ERR_ARG, "stage_ms: null job");
+  if (ms4)
+    for (int k = 0; k < 4; ++k) ms4[k] = j->stage_ms[k];
+  if (frames) *frames = j->stage_frames;
+  if (reset) {
+    for (double& v : j->stage_ms) v = 0.0;
+    j->stage_frames = 0;
+  }
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_amplitudes(mpsq_job* j, void** cs_dev) {
+  if (!j || !cs_dev) return fail(MPSQ_ERR_ARG, "amplitudes: null pointer");
+  *cs_dev = j->cs;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_sync(mpsq_job* j) {
+  if (!j) return fail(MPSQ_ERR_ARG, "sync: null job");
+  MPSQ_CUDA_TRY(cudaStreamSynchronize(j->s));
+  return check_dev_error(j->err, j->s);
+}
+
+// ---- accessor used by the time-axis unit
+namespace mpsq {
+JobView job_view(mpsq_job* j) {
+  JobView v;
+  v.precision = j->d.precision;
+  v.s = j->s;
+  v.cs = j->cs;
+  v.cs_species = j->cs_species;
+  v.n_q = j->g.n_modes;
+  v.n_frames = j->d.n_frames;
+  v.n_species = j->d.n_species;
+  return v;
+}
+}  // namespace mpsq

@@ -1,0 +1,510 @@
+// Time-axis kernels on the amplitude store cs(t, Q) of a job (frame-major, Q fastest):
+//  * total S(Q) = sum_t |cs|^2 / nfile                      (mp_sqom56.f90:1381-1387)
+//  * E=const map, sliding Hann window, one frequency bin     (:1437-1478, window :941-948)
+//  * E(Q) dispersion cut, windowed DFT per start frame       (:1480-1517)
+//  * Gaussian-window spectrum over the whole run (one FFT per Q, radix-2 in shared memory)
+// The ω-resolved forms subtract the elastic mean <cs>_t first (:1177-1185, :1359-1376) and
+// optionally scale by 1/|Q| (:1373).  Sums over frames are compensated (FP32) or FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mpsq_internal.h"
+
+namespace mpsq {
+
+template <typename T> struct Acc;  // compensated accumulator
+template <> struct Acc<float> {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <> struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <typename T>
+__global__ void sq_total_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+                                int nt, double scale, float* __restrict__ out) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  Acc<T> a;
+  for (int t = 0; t < nt; ++t) {
+    const auto v = cs[(int64_t)t * nq + q];
+    a.add(v.x * v.x + v.y * v.y);
+  }
+  out[q] = (float)(a.value() * scale);
+}
+
+// Loads a [nt x QT] tile of cs into shared memory, subtracts the column means and applies
+// the optional 1/|Q| factor.  Thread layout: column = tid % QT, part = tid / QT.
+template <typename T>
+__device__ void load_centered_tile(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+                                   int nt, int64_t q0, int QT, const float* __restrict__ q2n,
+                                   typename Cplx<T>::type* xs, T* red_re, T* red_im) {
+  using C = typename Cplx<T>::type;
+  const int tid = threadIdx.x, NT = blockDim.x;
+  for (int e = tid; e < nt * QT; e += NT) {
+    const int t = e / QT, c = e % QT;
+    const int64_t q = q0 + c;
+    C v;
+    v.x = 0;
+    v.y = 0;
+    if (q < nq) v = cs[(int64_t)t * nq + q];
+    xs[e] = v;
+  }
+  __syncthreads();
+  const int col = tid % QT, part = tid / QT, nparts = NT / QT;
+  T sr = 0, si = 0;
+  if (part < nparts)
+    for (int t = part; t < nt; t += nparts) {
+      sr += xs[t * QT + col].x;
+      si += xs[t * QT + col].y;
+    }
+  red_re[tid] = sr;
+  red_im[tid] = si;
+  __syncthreads();
+  if (tid < QT) {
+    T mr = 0, mi = 0;
+    for (int p = 0; p < nparts; ++p) {
+      mr += red_re[p * QT + tid];
+      mi += red_im[p * QT + tid];
+    }
+    red_re[NT + tid] = mr / (T)nt;
+    red_im[NT + tid] = mi / (T)nt;
+  }
+  __syncthreads();
+  for (int e = tid; e < nt * QT; e += NT) {
+    const int c = e % QT;
+    const int64_t q = q0 + c;
+    const T f = (q2n && q < nq) ? (T)q2n[q] : (T)1;
+    C v = xs[e];
+    v.x = (v.x - red_re[NT + c]) * f;
+    v.y = (v.y - red_im[NT + c]) * f;
+    xs[e] = v;
+  }
+  __syncthreads();
+}
+
+// E=const map: S(Q) = sum_{t0} | sum_i ph_i x(t0+i) |^2 with ph_i = t_wind_i exp(-2 pi i
+// (j_freq-1)(i - n_int/2)/n_int) (0-based i), times scale.
+template <typename T>
+__global__ void econst_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq, int nt,
+                              int QT, int n_int, const float* __restrict__ t_wind, int jf,
+                              const float* __restrict__ q2n, double scale,
+                              float* __restrict__ out) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int NT = blockDim.x;
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* ph = xs + (size_t)nt * QT;
+  T* red_re = reinterpret_cast<T*>(ph + n_int);
+  T* red_im = red_re + NT + QT;
+  const int64_t q0 = (int64_t)blockIdx.x * QT;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n_int; i += NT) {
+    const long long r = ((long long)jf * (long long)(i - n_int / 2)) % n_int;
+    T sn, cn;
+    if (sizeof(T) == 8) {
+      double s_, c_;
+      sincospi(-2.0 * (double)r / n_int, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    } else {
+      float s_, c_;
+      sincospif(-2.0f * (float)r / (float)n_int, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    }
+    C v;
+    v.x = cn * (T)t_wind[i];
+    v.y = sn * (T)t_wind[i];
+    ph[i] = v;
+  }
+  load_centered_tile<T>(cs, nq, nt, q0, QT, q2n, xs, red_re, red_im);
+  const int col = tid % QT, part = tid / QT, nparts = NT / QT;
+  const int n0 = nt - n_int + 1;
+  Acc<T> acc;
+  if (part < nparts)
+    for (int t0 = part; t0 < n0; t0 += nparts) {
+      T xr = 0, xi = 0;
+      for (int i = 0; i < n_int; ++i) {
+        const C a = ph[i], b = xs[(t0 + i) * QT + col];
+        xr += a.x * b.x - a.y * b.y;
+        xi += a.x * b.y + a.y * b.x;
+      }
+      acc.add(xr * xr + xi * xi);
+    }
+  __syncthreads();
+  red_re[tid] = (T)acc.value();
+  __syncthreads();
+  if (tid < QT) {
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p) s += (double)red_re[p * QT + tid];
+    const int64_t q = q0 + tid;
+    if (q < nq) out[q] = (float)(s * scale);
+  }
+}
+
+// Dispersion: for path point p (one CTA), acc[f] = sum_{t0} |sum_i w_i x(t0+i) e^{-2 pi i f i/n}|^2.
+template <typename T>
+__global__ void dispersion_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+                                  int nt, const int64_t* __restrict__ qidx, int n_int,
+                                  const float* __restrict__ t_wind, int n_freq,
+                                  const float* __restrict__ q2n, double scale,
+                                  float* __restrict__ out) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int NT = blockDim.x, tid = threadIdx.x;
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* tw = xs + nt;
+  T* red_re = reinterpret_cast<T*>(tw + n_int);
+  T* red_im = red_re + NT + 1;
+  const int64_t q = qidx[blockIdx.x];
+  if (q < 0 || q >= nq) {
+    for (int f = tid; f < n_freq; f += NT) out[(int64_t)blockIdx.x * n_freq + f] = 0.0f;
+    return;
+  }
+  for (int i = tid; i < n_int; i += NT) {
+    T sn, cn;
+    if (sizeof(T) == 8) {
+      double s_, c_;
+      sincospi(-2.0 * (double)i / n_int, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    } else {
+      float s_, c_;
+      sincospif(-2.0f * (float)i / (float)n_int, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    }
+    C v;
+    v.x = cn;
+    v.y = sn;
+    tw[i] = v;
+  }
+  // the column of this path point (QT = 1 tile)
+  load_centered_tile<T>(cs, nq, nt, q, 1, q2n, xs, red_re, red_im);
+  // window folded into the series once per start frame: x_w(i) = w_i x(t0+i)
+  const int n0 = nt - n_int + 1;
+  for (int f = tid; f < n_freq; f += NT) {
+    Acc<T> acc;
+    for (int t0 = 0; t0 < n0; ++t0) {
+      T xr = 0, xi = 0;
+      int r = 0;
+      for (int i = 0; i < n_int; ++i) {
+        const C b = xs[t0 + i];
+        const T wv = (T)t_wind[i];
+        const C a = tw[r];
+        xr += wv * (a.x * b.x - a.y * b.y);
+        xi += wv * (a.x * b.y + a.y * b.x);
+        r += f;
+        if (r >= n_int) r -= n_int;
+      }
+      acc.add(xr * xr + xi * xi);
+    }
+    out[(int64_t)blockIdx.x * n_freq + f] = (float)(acc.value() * scale);
+  }
+}
+
+// Gaussian-window spectrum: per Q column, X_k = sum_t g_t (x_t - <x>) e^{-2 pi i k t/nt},
+// out[k][q] = |X_k|^2 * scale for k < n_freq.  nt = 2^p <= 1024, radix-2 in shared memory.
+template <typename T>
+__global__ void gauss_fft_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+                                 int nt, int logn, int QT, const float* __restrict__ gwin,
+                                 int n_freq, const float* __restrict__ q2n, double scale,
+                                 float* __restrict__ out) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int NT = blockDim.x, tid = threadIdx.x;
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* tw = xs + (size_t)nt * QT;
+  T* red_re = reinterpret_cast<T*>(tw + nt / 2);
+  T* red_im = red_re + NT + QT;
+  const int64_t q0 = (int64_t)blockIdx.x * QT;
+  for (int i = tid; i < nt / 2; i += NT) {
+    T sn, cn;
+    if (sizeof(T) == 8) {
+      double s_, c_;
+      sincospi(-2.0 * (double)i / nt, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    } else {
+      float s_, c_;
+      sincospif(-2.0f * (float)i / (float)nt, &s_, &c_);
+      sn = (T)s_;
+      cn = (T)c_;
+    }
+    C v;
+    v.x = cn;
+    v.y = sn;
+    tw[i] = v;
+  }
+  load_centered_tile<T>(cs, nq, nt, q0, QT, q2n, xs, red_re, red_im);
+  // window
+  for (int e = tid; e < nt * QT; e += NT) {
+    const T g = (T)gwin[e / QT];
+    C v = xs[e];
+    v.x *= g;
+    v.y *= g;
+    xs[e] = v;
+  }
+  __syncthreads();
+  // bit reversal
+  for (int e = tid; e < nt * QT; e += NT) {
+    const int t = e / QT, c = e % QT;
+    const int r = (int)(__brev((unsigned)t) >> (32 - logn));
+    if (r > t) {
+      const C a = xs[t * QT + c];
+      xs[t * QT + c] = xs[r * QT + c];
+      xs[r * QT + c] = a;
+    }
+  }
+  __syncthreads();
+  const int nb = (nt / 2) * QT;
+  for (int s = 0; s < logn; ++s) {
+    const int half = 1 << s;
+    const int stride = nt >> (s + 1);  // twiddle index step
+    for (int e = tid; e < nb; e += NT) {
+      const int c = e % QT, b = e / QT;
+      const int grp = b >> s, pos = b & (half - 1);
+      const int i = (grp << (s + 1)) + pos, jj = i + half;
+      const C wv = tw[pos * stride];
+      const C u = xs[i * QT + c], v0 = xs[jj * QT + c];
+      C v;
+      v.x = v0.x * wv.x - v0.y * wv.y;
+      v.y = v0.x * wv.y + v0.y * wv.x;
+      C a, b2;
+      a.x = u.x + v.x;
+      a.y = u.y + v.y;
+      b2.x = u.x - v.x;
+      b2.y = u.y - v.y;
+      xs[i * QT + c] = a;
+      xs[jj * QT + c] = b2;
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n_freq * QT; e += NT) {
+    const int k = e / QT, c = e % QT;
+    const int64_t q = q0 + c;
+    if (q >= nq) continue;
+    const C v = xs[k * QT + c];
+    out[(int64_t)k * nq + q] = (float)((double)(v.x * v.x + v.y * v.y) * scale);
+  }
+}
+
+// ------------------------------------------------------------------------------- host
+static int tile_cols(int nt, size_t csz, size_t extra, size_t limit) {
+  int qt = 32;
+  while (qt > 1 && (size_t)nt * qt * csz + extra > limit) qt >>= 1;
+  if ((size_t)nt * qt * csz + extra > limit) return 0;
+  return qt;
+}
+
+struct OutBuf {
+  float* dev = nullptr;
+  bool owned = false;
+};
+
+static int out_prepare(float* out, int host, size_t n, OutBuf* b) {
+  if (!out) return fail(MPSQ_ERR_ARG, "null output pointer");
+  if (host) {
+    MPSQ_CUDA_TRY(cudaMalloc(&b->dev, std::max<size_t>(16, n * sizeof(float))));
+    b->owned = true;
+  } else {
+    b->dev = out;
+  }
+  return MPSQ_OK;
+}
+static int out_finish(float* out, int host, size_t n, OutBuf* b, cudaStream_t s) {
+  if (host) {
+    cudaError_t e = cudaMemcpyAsync(out, b->dev, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(b->dev);
+    if (e != cudaSuccess) return fail(MPSQ_ERR_CUDA, "output copy: %s", cudaGetErrorString(e));
+  }
+  return MPSQ_OK;
+}
+
+// Small host array -> temporary device copy.
+template <typename X>
+static int dev_copy(const X* h, size_t n, X** d, cudaStream_t s) {
+  *d = nullptr;
+  if (!h) return MPSQ_OK;
+  MPSQ_CUDA_TRY(cudaMalloc(d, std::max<size_t>(16, n * sizeof(X))));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(*d, h, n * sizeof(X), cudaMemcpyHostToDevice, s));
+  return MPSQ_OK;
+}
+
+}  // namespace mpsq
+
+using namespace mpsq;
+
+extern "C" int mpsq_job_sq_total(mpsq_job* j, double norm2, float* out, int host) {
+  if (!j) return fail(MPSQ_ERR_ARG, "sq_total: null job");
+  JobView v = job_view(j);
+  OutBuf b;
+  int rc = out_prepare(out, host, v.n_q, &b);
+  if (rc) return rc;
+  const double scale = 1.0 / ((double)v.n_frames * (norm2 > 0 ? norm2 : 1.0));
+  const unsigned nb = (unsigned)((v.n_q + 255) / 256);
+  if (v.precision == MPSQ_FP64)
+    sq_total_kernel<double><<<nb, 256, 0, v.s>>>((const double2*)v.cs, v.n_q, v.n_frames, scale, b.dev);
+  else
+    sq_total_kernel<float><<<nb, 256, 0, v.s>>>((const float2*)v.cs, v.n_q, v.n_frames, scale, b.dev);
+  MPSQ_LAUNCH_CHECK();
+  return out_finish(out, host, v.n_q, &b, v.s);
+}
+
+// q2_norm and t_wind are host arrays (n_Q and n_int floats).
+extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                   int32_t j_freq, const float* q2_norm, double scale,
+                                   float* out, int host) {
+  if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst: null pointer");
+  JobView v = job_view(j);
+  if (n_int < 1 || n_int > v.n_frames)
+    return fail(MPSQ_ERR_ARG, "sqw_econst: n_int %d outside 1..n_frames (%d)", n_int, v.n_frames);
+  if (j_freq < 1) return fail(MPSQ_ERR_ARG, "sqw_econst: j_freq must be >= 1");
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const int NT = 256;
+  const size_t extra = (size_t)n_int * csz + (size_t)2 * (NT + 32) * (csz / 2);
+  const int QT = tile_cols(v.n_frames, csz, extra, 200 * 1024);
+  if (QT == 0) return fail(MPSQ_ERR_ARG, "sqw_econst: %d frames do not fit in shared memory", v.n_frames);
+  const size_t smem = (size_t)v.n_frames * QT * csz + (size_t)n_int * csz + (size_t)2 * (NT + QT) * (csz / 2);
+  float *dw = nullptr, *dq = nullptr;
+  int rc = dev_copy(t_wind, n_int, &dw, v.s);
+  if (!rc) rc = dev_copy(q2_norm, q2_norm ? v.n_q : 0, &dq, v.s);
+  OutBuf b;
+  if (!rc) rc = out_prepare(out, host, v.n_q, &b);
+  if (rc) {
+    cudaFree(dw);
+    cudaFree(dq);
+    return rc;
+  }
+  const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
+  const int jf = j_freq - 1;
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(econst_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    econst_kernel<double><<<nb, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, v.n_frames, QT, n_int,
+                                                 dw, jf, dq, scale, b.dev);
+  } else {
+    cudaFuncSetAttribute(econst_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    econst_kernel<float><<<nb, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, v.n_frames, QT, n_int, dw,
+                                                jf, dq, scale, b.dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  rc = e == cudaSuccess ? out_finish(out, host, v.n_q, &b, v.s)
+                        : fail(MPSQ_ERR_CUDA, "econst launch: %s", cudaGetErrorString(e));
+  cudaStreamSynchronize(v.s);
+  cudaFree(dw);
+  cudaFree(dq);
+  return rc;
+}
+
+extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                       int32_t n_path, const int64_t* q_index, int32_t n_freq,
+                                       const float* q2_norm, double scale, float* out,
+                                       int host) {
+  if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion: null pointer");
+  JobView v = job_view(j);
+  if (n_int < 1 || n_int > v.n_frames) return fail(MPSQ_ERR_ARG, "sqw_dispersion: bad n_int");
+  if (n_path < 1 || n_freq < 1 || n_freq > n_int) return fail(MPSQ_ERR_ARG, "sqw_dispersion: bad sizes");
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const int NT = 128;
+  const size_t smem = (size_t)v.n_frames * csz + (size_t)n_int * csz + (size_t)2 * (NT + 2) * (csz / 2);
+  if (smem > 200 * 1024) return fail(MPSQ_ERR_ARG, "sqw_dispersion: too many frames");
+  float *dw = nullptr, *dq = nullptr;
+  int64_t* di = nullptr;
+  int rc = dev_copy(t_wind, n_int, &dw, v.s);
+  if (!rc) rc = dev_copy(q2_norm, q2_norm ? v.n_q : 0, &dq, v.s);
+  if (!rc) rc = dev_copy(q_index, n_path, &di, v.s);
+  OutBuf b;
+  if (!rc) rc = out_prepare(out, host, (size_t)n_path * n_freq, &b);
+  if (rc) {
+    cudaFree(dw);
+    cudaFree(dq);
+    cudaFree(di);
+    return rc;
+  }
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(dispersion_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    dispersion_kernel<double><<<n_path, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, v.n_frames, di,
+                                                         n_int, dw, n_freq, dq, scale, b.dev);
+  } else {
+    cudaFuncSetAttribute(dispersion_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    dispersion_kernel<float><<<n_path, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, v.n_frames, di,
+                                                        n_int, dw, n_freq, dq, scale, b.dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_path * n_freq, &b, v.s)
+                        : fail(MPSQ_ERR_CUDA, "dispersion launch: %s", cudaGetErrorString(e));
+  cudaStreamSynchronize(v.s);
+  cudaFree(dw);
+  cudaFree(dq);
+  cudaFree(di);
+  return rc;
+}
+
+extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_freq,
+                                  const float* q2_norm, double scale, float* out, int host) {
+  if (!j) return fail(MPSQ_ERR_ARG, "sqw_gauss: null job");
+  JobView v = job_view(j);
+  const int nt = v.n_frames;
+  if (nt < 2 || nt > 1024 || (nt & (nt - 1)))
+    return fail(MPSQ_ERR_ARG, "sqw_gauss: n_frames (%d) must be a power of two in 2..1024", nt);
+  if (n_freq < 1 || n_freq > nt) return fail(MPSQ_ERR_ARG, "sqw_gauss: n_freq outside 1..n_frames");
+  if (!(fwhm_frames > 0)) return fail(MPSQ_ERR_ARG, "sqw_gauss: fwhm must be > 0");
+  int logn = 0;
+  while ((1 << logn) < nt) ++logn;
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const int NT = 256;
+  const size_t extra = (size_t)(nt / 2) * csz + (size_t)2 * (NT + 32) * (csz / 2);
+  const int QT = tile_cols(nt, csz, extra, 160 * 1024);
+  if (QT == 0) return fail(MPSQ_ERR_ARG, "sqw_gauss: tile does not fit");
+  const size_t smem = (size_t)nt * QT * csz + (size_t)(nt / 2) * csz + (size_t)2 * (NT + QT) * (csz / 2);
+  std::vector<float> g(nt);
+  const double tc = 0.5 * (nt - 1);
+  for (int t = 0; t < nt; ++t) {
+    const double u = (t - tc) / fwhm_frames;
+    g[t] = (float)std::exp(-4.0 * std::log(2.0) * u * u);
+  }
+  float *dg = nullptr, *dq = nullptr;
+  int rc = dev_copy(g.data(), nt, &dg, v.s);
+  if (!rc) rc = dev_copy(q2_norm, q2_norm ? v.n_q : 0, &dq, v.s);
+  OutBuf b;
+  if (!rc) rc = out_prepare(out, host, (size_t)n_freq * v.n_q, &b);
+  if (rc) {
+    cudaFree(dg);
+    cudaFree(dq);
+    return rc;
+  }
+  const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(gauss_fft_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    gauss_fft_kernel<double><<<nb, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, nt, logn, QT, dg,
+                                                    n_freq, dq, scale, b.dev);
+  } else {
+    cudaFuncSetAttribute(gauss_fft_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    gauss_fft_kernel<float><<<nb, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, nt, logn, QT, dg,
+                                                   n_freq, dq, scale, b.dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_freq * v.n_q, &b, v.s)
+                        : fail(MPSQ_ERR_CUDA, "gauss launch: %s", cudaGetErrorString(e));
+  cudaStreamSynchronize(v.s);
+  cudaFree(dg);
+  cudaFree(dq);
+  return rc;
+}

@@ -1,0 +1,413 @@
+"""Host-side mirror of mp_sqom's operator interface for the S(Q,omega) path.
+
+``QGrid`` restates the Q-grid geometry of mp_sqom (code/src/mp_sqom56.f90:764-936): plane
+vectors, phase scales tpe, pixel counts n_qx/n_qy (even), Q centre, the 1/|Q| table and the
+physical-Q vectors the X-ray form factors use — in FP32 where the reference stores real(4).
+The optional third axis (ndim=3) extends the plane to a volume along ev with the same rules.
+
+``TimeAxis`` restates the time constants (:680-704) and windows (:941-948).
+
+``SqomJob`` drives libmpsq's job API: trajectory upload, the frame loop on the GPU, and the
+maps of plot_loop (total S(Q), E=const, E(Q) dispersion) plus the whole-run Gaussian spectrum,
+normalised as the reference normalises them (:1527, :1573-1576).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr
+
+TWOPI = 2.0 * np.pi
+f32 = np.float32
+
+
+def _dot32(a, b):
+    a = np.asarray(a, f32)
+    b = np.asarray(b, f32)
+    s = f32(0)
+    for i in range(3):
+        s = f32(s + f32(a[i] * b[i]))
+    return s
+
+
+def _norm32(a):
+    return f32(np.sqrt(_dot32(a, a)))
+
+
+def _matvec32(m, v):
+    m = np.asarray(m, f32)
+    return np.array([_dot32(m[i], v) for i in range(3)], f32)
+
+
+@dataclass
+class QGrid:
+    """Q grid of one map (mp_sqom56.f90:764-936)."""
+    input_method: int                 # _lib.CELL or _lib.BULK
+    n_row: tuple                      # supercell (1,1,1 for BULK boxes)
+    e1: tuple = (1, 0, 0)
+    e2: tuple = (0, 1, 0)
+    n_bz: float = 1.0                 # Brillouin zones (CELL) or Q-range in 1/A (BULK)
+    q_center: tuple = (0.0, 0.0, 0.0)
+    a_par: tuple = (1.0, 1.0, 1.0)
+    a_cell_inv: np.ndarray | None = None
+    ndim: int = 2
+    at_pos_min: tuple | None = None
+    at_pos_max: tuple | None = None
+    at_pos_centre: tuple = (0.0, 0.0, 0.0)
+
+    def __post_init__(self):
+        n_row = np.asarray(self.n_row, np.int64)
+        self.nsuper = int(np.prod(n_row))
+        a_par = np.asarray(self.a_par, f32)
+        if self.at_pos_min is None:
+            if self.nsuper == 1:
+                self.at_pos_min = tuple(-a_par / 2)
+                self.at_pos_max = tuple(a_par / 2)
+            else:
+                self.at_pos_min = tuple((-n_row / 2.0).astype(f32))
+                self.at_pos_max = tuple((n_row / 2.0).astype(f32))
+        if self.a_cell_inv is None:
+            # CELL: reciprocal of the orthogonal cell (:529-534 without data_header_3);
+            # BULK boxes: the identity that BULK .dat headers carry (positions in Angstrom).
+            self.a_cell_inv = (np.diag(1.0 / a_par) if self.nsuper > 1 else np.eye(3)).astype(f32)
+        e1 = np.asarray(self.e1, f32)
+        e2 = np.asarray(self.e2, f32)
+        ev = np.array([e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                       e1[0] * e2[1] - e1[1] * e2[0]], f32)
+        self.e1_norm, self.e2_norm, self.ev_norm = _norm32(e1), _norm32(e2), _norm32(ev)
+        e1n = (e1 / self.e1_norm).astype(f32)
+        e2n = (e2 / self.e2_norm).astype(f32)
+        evn = (ev / self.ev_norm).astype(f32)
+        self.axis = np.stack([e1n, e2n, evn])
+        span = (np.asarray(self.at_pos_max, f32) - np.asarray(self.at_pos_min, f32)).astype(f32)
+        # tpe = twopi (real 8) / real(4) dot product, stored as real(4) (:809-811); the plane
+        # normal's scale is unused by a 2D map (the reference divides by zero there for
+        # e.g. (hhl) planes of a cubic box)
+        spans = [float(_dot32(a, span)) for a in self.axis]
+        if any(s == 0.0 for s in spans[:self.ndim]):
+            raise ValueError("box has zero extent along a Q axis: choose other plane vectors")
+        self.tpe = np.array([f32(TWOPI / s) if s != 0.0 else f32(0.0) for s in spans], f32)
+        scale = TWOPI if self.nsuper > 1 else 1.0
+        self.ep = np.stack([(scale * _matvec32(self.a_cell_inv, a).astype(np.float64)).astype(f32)
+                            for a in self.axis])
+        e1p_n, e2p_n = _norm32(self.ep[0]), _norm32(self.ep[1])
+        self.evp_norm = _norm32(self.ep[2])
+        cos_ep = f32(_dot32(self.ep[0], self.ep[1]) / (e1p_n * e1p_n))
+        bz_n = f32(self.n_bz)
+        if self.nsuper > 1:
+            bz_ny = max(bz_n, f32(bz_n * (e1p_n / (e2p_n * f32(np.sqrt(f32(1.0) - cos_ep ** 2))))))
+            bz_nx = f32(bz_n + bz_ny * abs(cos_ep)) if abs(cos_ep) > 0 else bz_n
+            bz_nz = bz_n
+            n = [int(TWOPI * float(b) / float(t)) if t != 0 else 1
+                 for b, t in zip((bz_nx, bz_ny, bz_nz), self.tpe)]
+        else:
+            bz_nx = bz_ny = bz_nz = bz_n
+            n = [int(f32(b / t)) if t != 0 else 1 for b, t in zip((bz_nx, bz_ny, bz_nz), self.tpe)]
+        n = [k + 1 if (k > 1 and k % 2) else k for k in n]
+        n = [max(1, k) for k in n]
+        if self.ndim == 2:
+            n[2] = 1
+        self.n_q = tuple(n)
+        self.bz = np.array([bz_nx, bz_ny, bz_nz], f32)
+        qc = np.asarray(self.q_center, f32)
+        norms = (self.e1_norm, self.e2_norm, self.ev_norm)
+        centre = np.array([f32(_dot32(self.axis[k], qc) / norms[k]) for k in range(3)], f32)
+        self.q_min = np.array([centre[k] - f32(0.5) * self.bz[k] if self.n_q[k] > 1 else centre[k]
+                               for k in range(3)], f32)
+        self.dq = np.array([f32(self.bz[k] / self.n_q[k]) for k in range(3)], f32)
+        self.q_v = (centre[2] * evn).astype(f32)  # out-of-plane part of q_center (:900)
+        self.q_vp = (f32(_dot32(self.ep[2], qc) / self.evp_norm) * self.ep[2]).astype(f32)
+
+    @property
+    def shape(self):
+        """Array shape of a map, slowest axis first: (n_qz, n_qy, n_qx)."""
+        return (self.n_q[2], self.n_q[1], self.n_q[0])
+
+    @property
+    def n_modes(self) -> int:
+        return int(np.prod(self.n_q))
+
+    def axis_values(self, k):
+        """Q coordinate along axis k of pixel i = 0..n-1 (r.l.u. or 1/A)."""
+        return (self.q_min[k] + np.arange(self.n_q[k], dtype=f32) * self.dq[k]).astype(f32)
+
+    def q2_norm(self) -> np.ndarray:
+        """1/|Q| table (:904-917), Q in r.l.u. (CELL) or 1/A (BULK); flattened, x fastest."""
+        qx, qy = self.axis_values(0), self.axis_values(1)
+        q = (qx[None, None, :, None] * self.axis[0][None, None, None, :]
+             + qy[None, :, None, None] * self.axis[1][None, None, None, :])
+        if self.ndim == 3:
+            qz = self.axis_values(2)
+            q = q + qz[:, None, None, None] * self.axis[2][None, None, None, :]
+            extra = f32(0)
+        else:
+            extra = _dot32(self.q_v, self.q_v)
+        qsq = (q.astype(f32) ** 2).sum(-1).astype(f32) + extra
+        out = np.where(qsq >= 1e-8, 1.0 / np.sqrt(np.maximum(qsq, 1e-30)), 1.0).astype(f32)
+        return out.reshape(-1)
+
+    def qphys(self):
+        """(origin, steps[3], extra_sq) with Q_phys(k) = origin + sum_a k_a steps[a] for mode k
+        (k_a = i_a - n_a/2) — the vector mp_sqom feeds to the form factors (:919-931)."""
+        origin = np.zeros(3, np.float64)
+        steps = np.zeros((3, 3), np.float64)
+        for k in range(self.ndim):
+            origin += float(self.q_min[k] + (self.n_q[k] // 2) * self.dq[k]) * self.ep[k].astype(np.float64)
+            steps[k] = float(self.dq[k]) * self.ep[k].astype(np.float64)
+        extra = float(_dot32(self.q_vp, self.q_vp)) if self.ndim == 2 else 0.0
+        return origin, steps, extra
+
+
+@dataclass
+class TimeAxis:
+    """Time constants and Hann window (mp_sqom56.f90:680-704, :941-948)."""
+    nfile: int
+    t_step: float
+    n_int: int = 0
+    j_sq: int = 1
+
+    def __post_init__(self):
+        if self.n_int == 0:
+            self.n_int = self.nfile // 2
+        if self.j_sq == 1 and self.n_int % 2 == 0:
+            self.n_int += 1
+        self.n_int = max(1, min(self.n_int, self.nfile))
+        self.freq_step = 1.0 / ((self.n_int - 1) * self.t_step) if self.n_int > 1 else 0.0
+        self.n_freq_max = (self.n_int - 1) // 2 + 1
+        self.n_frame = self.nfile - self.n_int + 1
+
+    def window(self) -> np.ndarray:
+        if self.n_int <= 1:
+            return np.ones(self.n_int, f32)
+        i = np.arange(1, self.n_int + 1, dtype=np.float64)
+        return (0.5 * (1.0 - np.cos(TWOPI * (i - 1) / (self.n_int - 1)))).astype(f32)
+
+
+class SqomJob:
+    """One S(Q,omega) job on the GPU (device-resident trajectory, amplitudes and grids)."""
+
+    def __init__(self, grid: QGrid, *, species_counts, n_frames: int, precision: int = _lib.FP32,
+                 eps: float = 1e-6, weight_mode: int = _lib.WEIGHT_UNIT, b_coh=None, xff=None,
+                 ff_convention: int = _lib.FF_MP_SQOM, mask=None, window: bool = False,
+                 phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
+                 n_atoms_frame: int | None = None, use_range: bool = False, eps_x: float = 0.1,
+                 stream: int | None = None):
+        L = _lib.load()
+        self.grid = grid
+        self.species_counts = [int(n) for n in species_counts]
+        S = len(self.species_counts)
+        if S < 1 or S > _lib.MAX_SPECIES:
+            raise ValueError("1..16 species supported")
+        d = _lib.JobDesc()
+        d.ndim = grid.ndim
+        d.precision = precision
+        d.eps = eps
+        for k in range(3):
+            d.n_modes[k] = grid.n_q[k]
+            d.tpe[k] = float(grid.tpe[k])
+            d.centre[k] = float(grid.at_pos_centre[k])
+            d.pos_min[k] = float(grid.at_pos_min[k])
+            d.pos_max[k] = float(grid.at_pos_max[k])
+            d.n_row[k] = int(grid.n_row[k])
+            d.q_center[k] = float(grid.q_center[k])
+            for b in range(3):
+                d.axis[k][b] = float(grid.axis[k][b])
+        d.input_method = grid.input_method
+        d.phase_rounding = int(phase_rounding)
+        d.use_range = int(use_range)
+        d.eps_x = eps_x
+        d.bulk_nsuper1 = int(grid.nsuper == 1)
+        d.spatial_window = int(window)
+        d.n_species = S
+        off = np.concatenate([[0], np.cumsum(self.species_counts)])
+        for s in range(S + 1):
+            d.species_offset[s] = int(off[s])
+        mask = [1] * S if mask is None else list(mask)
+        for s in range(S):
+            d.mask[s] = int(mask[s])
+        d.weight_mode = weight_mode
+        if b_coh is not None:
+            for s in range(S):
+                d.b_coh[s] = float(b_coh[s])
+        if xff is not None:
+            for s in range(S):
+                for i in range(9):
+                    d.xff[s][i] = float(xff[s][i])
+        d.ff_convention = ff_convention
+        origin, steps, extra = grid.qphys()
+        for b in range(3):
+            d.qphys_origin[b] = origin[b]
+            for k in range(3):
+                d.qphys_step[k][b] = steps[k][b]
+        d.qphys_extra_sq = extra
+        d.n_atoms_frame = int(n_atoms_frame if n_atoms_frame is not None else off[-1])
+        d.n_frames = int(n_frames)
+        d.store_species = int(store_species)
+        d.no_pack = int(no_pack)
+        self.desc = d
+        self.n_frames = int(n_frames)
+        self.n_atoms_frame = d.n_atoms_frame
+        self.precision = precision
+        self._h = C.c_void_p()
+        check(L.mpsq_job_create(C.byref(d), C.c_void_p(stream or 0), C.byref(self._h)), "job_create")
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if self._h:
+            _lib.load().mpsq_job_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def estimate_bytes(desc) -> int:
+        b = C.c_int64()
+        check(_lib.load().mpsq_job_estimate_bytes(C.byref(desc), C.byref(b)), "estimate_bytes")
+        return int(b.value)
+
+    # ------------------------------------------------------------------ inputs
+    def set_frames(self, pos, first: int = 0):
+        """pos: (count, n_atoms_frame, 4) float32, numpy (host) or torch CUDA tensor."""
+        host = not (hasattr(pos, "is_cuda") and pos.is_cuda)
+        if host:
+            pos = np.ascontiguousarray(pos, dtype=np.float32)
+        count = pos.shape[0] if pos.ndim == 3 else 1
+        if pos.shape[-2] != self.n_atoms_frame or pos.shape[-1] != 4:
+            raise ValueError("frames must be (count, n_atoms_frame, 4)")
+        check(_lib.load().mpsq_job_set_frames(self._h, C.c_void_p(ptr(pos)), first, count, int(host)),
+              "set_frames")
+        self._keep = pos  # keep host memory alive until the copy is ordered
+
+    def set_cell_index(self, at_ind):
+        a = np.ascontiguousarray(at_ind, dtype=np.int32)
+        check(_lib.load().mpsq_job_set_cell_index(self._h, C.c_void_p(ptr(a)), 1), "set_cell_index")
+        self.sync()
+
+    # ------------------------------------------------------------------ compute
+    def transform(self, first: int = 0, count: int | None = None):
+        count = self.n_frames - first if count is None else count
+        check(_lib.load().mpsq_job_transform(self._h, first, count), "transform")
+
+    def sync(self):
+        check(_lib.load().mpsq_job_sync(self._h), "sync")
+
+    def profile(self, enable: bool = True):
+        check(_lib.load().mpsq_job_profile(self._h, int(enable)), "profile")
+
+    def stage_ms(self, reset: bool = False):
+        """Accumulated [bin, spread, fft, deconv] milliseconds and frames timed."""
+        ms = (C.c_double * 4)()
+        fr = C.c_int64()
+        check(_lib.load().mpsq_job_stage_ms(self._h, ms, C.byref(fr), int(reset)), "stage_ms")
+        return list(ms), int(fr.value)
+
+    def amplitudes_ptr(self) -> int:
+        p = C.c_void_p()
+        check(_lib.load().mpsq_job_amplitudes(self._h, C.byref(p)), "amplitudes")
+        return int(p.value or 0)
+
+    def amplitudes(self) -> np.ndarray:
+        """cs(t,Q) copied to the host, shape (n_frames, n_Q), complex64/complex128."""
+        import torch
+        n = self.n_frames * self.grid.n_modes
+        dt = torch.complex128 if self.precision == _lib.FP64 else torch.complex64
+        out = torch.empty(n, dtype=dt)
+        self.sync()
+        src = self.amplitudes_ptr()
+        nbytes = out.element_size() * n
+        cudart = _cudart()
+        check_rt(cudart.cudaMemcpy(C.c_void_p(out.data_ptr()), C.c_void_p(src), C.c_size_t(nbytes), 2),
+                 "cudaMemcpy")
+        return out.numpy().reshape(self.n_frames, -1)
+
+    def norm2(self) -> float:
+        return float(sum(self.species_counts)) ** 2
+
+    def sq_total(self, normalize: bool = True, out=None) -> np.ndarray:
+        """Total S(Q) = <|cs|^2>_t / (sum N_j)^2 (:1381-1387, :1573-1574)."""
+        n2 = self.norm2() if normalize else 1.0
+        host = out is None or not hasattr(out, "is_cuda")
+        res = np.empty(self.grid.n_modes, f32) if out is None else out
+        check(_lib.load().mpsq_job_sq_total(self._h, n2, C.c_void_p(ptr(res)), int(host)), "sq_total")
+        return res
+
+    def sqw_econst(self, taxis: TimeAxis, j_freq: int, q2_norm=None, normalize=True,
+                   t_wind=None) -> np.ndarray:
+        """E=const map for 1-based bin j_freq (:1437-1478), normalised as :1527, :1575-1576."""
+        w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
+        q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
+        scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
+        if normalize:
+            scale *= taxis.t_step / self.norm2()
+        res = np.empty(self.grid.n_modes, f32)
+        check(_lib.load().mpsq_job_sqw_econst(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
+                                              C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
+              "sqw_econst")
+        return res
+
+    def sqw_dispersion(self, taxis: TimeAxis, q_index, n_freq=None, q2_norm=None,
+                       normalize=True, t_wind=None) -> np.ndarray:
+        """E(Q) cut along pixel indices q_index (:1480-1517); returns (n_path, n_freq)."""
+        w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
+        qi = np.ascontiguousarray(q_index, np.int64)
+        n_freq = taxis.n_freq_max if n_freq is None else n_freq
+        q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
+        scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
+        if normalize:
+            scale *= taxis.t_step / self.norm2()
+        res = np.empty((len(qi), n_freq), f32)
+        check(_lib.load().mpsq_job_sqw_dispersion(self._h, taxis.n_int, C.c_void_p(ptr(w)), len(qi),
+                                                  C.c_void_p(ptr(qi)), n_freq, C.c_void_p(ptr(q2)),
+                                                  scale, C.c_void_p(ptr(res)), 1), "sqw_dispersion")
+        return res
+
+    def sqw_gauss(self, fwhm_frames=None, n_freq=None, t_step=1.0, q2_norm=None, normalize=True,
+                  out=None) -> np.ndarray:
+        """Whole-run Gaussian-window spectrum, (n_freq, n_Q); normalised by sum(g) * t_step /
+        (sum N)^2 like the sliding-window maps."""
+        F = self.n_frames
+        fwhm = F / 2 if fwhm_frames is None else fwhm_frames
+        n_freq = F // 2 + 1 if n_freq is None else n_freq
+        g = np.exp(-4.0 * np.log(2.0) * ((np.arange(F) - 0.5 * (F - 1)) / fwhm) ** 2)
+        scale = 1.0 / g.sum()
+        if normalize:
+            scale *= t_step / self.norm2()
+        q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
+        host = out is None or not hasattr(out, "is_cuda")
+        res = np.empty((n_freq, self.grid.n_modes), f32) if out is None else out
+        check(_lib.load().mpsq_job_sqw_gauss(self._h, float(fwhm), n_freq, C.c_void_p(ptr(q2)),
+                                             scale, C.c_void_p(ptr(res)), int(host)), "sqw_gauss")
+        return res
+
+
+_rt = None
+
+
+def _cudart():
+    global _rt
+    if _rt is None:
+        import glob
+        import os
+        cands = sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+        _rt = C.CDLL(cands[0] if cands else "libcudart.so")
+        _rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    return _rt
+
+
+def check_rt(code, where):
+    if code != 0:
+        raise RuntimeError(f"{where}: cuda error {code}")

@@ -1,0 +1,160 @@
+"""ORACLE — test infrastructure only (see oracle/__init__.py).
+
+numpy restatement of the loops of MP_TOOLS mp_sqom around the NUFFT call, each function citing
+the reference lines it follows (paths relative to the MP_TOOLS tree):
+
+  prep_points      code/src/mp_sqom56.f90:1100-1143  selection, phases x,y(,z), strengths
+  weighted_sum     code/src/mp_sqom56.f90:1338-1377  species weights, elastic mean, 1/|Q|
+  sq_total         code/src/mp_sqom56.f90:1381-1387  S(Q) = <|cs|^2>_t
+  hann_window      code/src/mp_sqom56.f90:941-948    t_wind
+  econst           code/src/mp_sqom56.f90:1437-1478  sliding-window E=const map
+  dispersion       code/src/mp_sqom56.f90:1480-1517  E(Q) cut, FFT per start frame
+  gauss_spectrum   whole-run Gaussian window + one DFT per Q (the benchmark's time transform)
+  xray_ff          code/src/mp_sqom56.f90:919-936 (and mp_sql56.f90:1048-1058 convention)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def prep_points(frame, lo, hi, *, input_method, ndim, axis, tpe, centre, q_center,
+                window=False, phase_rounding=False, use_range=False, at_ind=None,
+                n_row=(1, 1, 1), pos_min=None, pos_max=None, tol=0.1):
+    """Points of one species (atoms lo..hi of frame, float32 (N,4)).  Returns the list of
+    coordinate arrays (radians, FP64) and complex128 strengths, after the reference's
+    selection: CELL skips atoms at exactly (0,0,0) (:1107) and, with use_range, cells outside
+    [pos_min, pos_max] (:1108-1111); BULK keeps atoms within the box +- tol (:1121-1128)."""
+    r = np.asarray(frame[lo:hi, :3], dtype=np.float32)
+    keep = np.ones(len(r), bool)
+    if input_method == 0:
+        keep &= ~((r[:, 0] == 0) & (r[:, 1] == 0) & (r[:, 2] == 0))
+        if use_range and at_ind is not None:
+            ci = np.asarray(at_ind[lo:hi, :3]) - (np.asarray(n_row) // 2) - 1
+            keep &= np.all((ci >= np.asarray(pos_min)) & (ci <= np.asarray(pos_max)), axis=1)
+    else:
+        pmin = np.asarray(pos_min, np.float32)
+        pmax = np.asarray(pos_max, np.float32)
+        t = np.float32(tol)
+        keep &= np.all((r >= pmin - t) & (r < pmax + t), axis=1)
+    r = r[keep]
+    coords = []
+    for k in range(ndim):
+        if phase_rounding:
+            ax = np.asarray(axis[k], np.float32)
+            d = (r - np.asarray(centre, np.float32)).astype(np.float32)
+            pr = np.float32(0.0) * d[:, 0]
+            for b in range(3):
+                pr = (pr + (ax[b] * d[:, b]).astype(np.float32)).astype(np.float32)
+            coords.append((pr * np.float32(tpe[k])).astype(np.float32).astype(np.float64))
+        else:
+            d = r.astype(np.float64) - np.asarray(centre, np.float64)
+            coords.append((d @ np.asarray(axis[k], np.float64)) * float(tpe[k]))
+    qc = np.asarray(q_center, np.float64)
+    if np.any(qc != 0):
+        if phase_rounding:
+            tq = (np.float32(2 * np.pi) * qc.astype(np.float32)).astype(np.float32)
+            arg = np.zeros(len(r), np.float32)
+            for b in range(3):
+                arg = (arg + (tq[b] * r[:, b]).astype(np.float32)).astype(np.float32)
+            c = np.exp(-1j * arg.astype(np.float64))
+        else:
+            turns = r.astype(np.float64) @ qc
+            c = np.exp(-2j * np.pi * (turns - np.floor(turns)))
+    else:
+        c = np.ones(len(r), np.complex128)
+    if window:
+        nw = 2 if ndim == 2 else 3
+        for k in range(nw):
+            c = c * (1.0 + np.cos(coords[k]))
+    return coords, c
+
+
+def xray_ff(xff, qsq_kappa):
+    """f = c + sum_i a_i exp(-b_i * s2) with s2 = kappa |Q|^2, xff = (a1 b1 .. a4 b4 c)."""
+    xff = np.asarray(xff, np.float64)
+    f = np.full_like(qsq_kappa, xff[8], dtype=np.float64)
+    for i in range(4):
+        f = f + xff[2 * i] * np.exp(-xff[2 * i + 1] * qsq_kappa)
+    return f
+
+
+def weighted_sum(amps, weights, mask=None, wnorm=1.0):
+    """cs(t,Q) = sum_j mask_j w_j(Q) A_j(t,Q) (:1338-1356).  amps (F, S, nQ), weights (S, nQ)
+    or (S,)."""
+    amps = np.asarray(amps)
+    S = amps.shape[1]
+    mask = np.ones(S) if mask is None else np.asarray(mask)
+    w = np.asarray(weights, np.float64)
+    if w.ndim == 1:
+        w = w[:, None]
+    cs = np.zeros((amps.shape[0], amps.shape[2]), np.complex128)
+    for j in range(S):
+        if mask[j]:
+            cs += w[j][None, :] * amps[:, j, :]
+    return cs * wnorm
+
+
+def centered(cs, q2_norm=None):
+    """cs - <cs>_t (mean over frames, :1177-1185), times 1/|Q| if given (:1373)."""
+    x = cs - cs.mean(axis=0, keepdims=True)
+    if q2_norm is not None:
+        x = x * np.asarray(q2_norm)[None, :]
+    return x
+
+
+def sq_total(cs, norm2=1.0):
+    """S(Q) = sum_t |cs|^2 / nfile / norm2 (:1381-1387, :1573-1574)."""
+    return (np.abs(cs) ** 2).sum(axis=0) / cs.shape[0] / norm2
+
+
+def hann_window(n_int, variant="symmetric"):
+    """t_wind of :941-948 ('symmetric', denominator n_int-1) or of :2429-2431 ('options')."""
+    i = np.arange(1, n_int + 1, dtype=np.float64)
+    if n_int <= 1:
+        return np.ones(n_int)
+    if variant == "symmetric":
+        return 0.5 * (1.0 - np.cos(2 * np.pi * (i - 1) / (n_int - 1)))
+    return 0.5 * (1.0 - np.cos(2 * np.pi * i / (n_int + 1)))
+
+
+def econst(cs, n_int, t_wind, j_freq, q2_norm=None, scale=1.0):
+    """E=const map for 1-based bin j_freq (:1437-1478): sum over start frames of
+    |sum_i om_phase_i x(t0+i)|^2, om_phase_i = t_wind_i exp(-2 pi i (j_freq-1)(i-n_int/2-1)/n_int)."""
+    x = centered(cs, q2_norm)
+    F = x.shape[0]
+    i = np.arange(1, n_int + 1)
+    ph = np.asarray(t_wind) * np.exp(-2j * np.pi * (j_freq - 1) * (i - n_int // 2 - 1) / n_int)
+    n0 = F - n_int + 1
+    out = np.zeros(x.shape[1])
+    for t0 in range(n0):
+        X = ph @ x[t0:t0 + n_int]
+        out += np.abs(X) ** 2
+    return out * scale
+
+
+def dispersion(cs, n_int, t_wind, q_index, n_freq, q2_norm=None, scale=1.0):
+    """E(Q) cut (:1480-1517): for each path index, sum over start frames of
+    |FFT(t_wind * x(t0 : t0+n_int))[0:n_freq]|^2 (forward, unscaled).  Returns (n_path, n_freq)."""
+    x = centered(cs, q2_norm)[:, np.asarray(q_index)]
+    F = x.shape[0]
+    n0 = F - n_int + 1
+    out = np.zeros((x.shape[1], n_freq))
+    w = np.asarray(t_wind)[:, None]
+    for t0 in range(n0):
+        X = np.fft.fft(w * x[t0:t0 + n_int], axis=0)[:n_freq]
+        out += (np.abs(X) ** 2).T
+    return out * scale
+
+
+def gauss_window(n_frames, fwhm):
+    t = np.arange(n_frames)
+    tc = 0.5 * (n_frames - 1)
+    return np.exp(-4.0 * np.log(2.0) * ((t - tc) / fwhm) ** 2)
+
+
+def gauss_spectrum(cs, fwhm, n_freq, q2_norm=None, scale=1.0):
+    """|sum_t g_t (cs_t - <cs>) exp(-2 pi i k t / F)|^2 for k < n_freq; returns (n_freq, nQ)."""
+    x = centered(cs, q2_norm)
+    g = gauss_window(x.shape[0], fwhm)[:, None]
+    X = np.fft.fft(g * x, axis=0)[:n_freq]
+    return np.abs(X) ** 2 * scale

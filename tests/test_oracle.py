@@ -1,0 +1,119 @@
+"""Oracle self-checks against known answers (CPU only)."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import sqom_ref
+
+
+def test_single_atom_at_origin_gives_unit_amplitudes():
+    f = oracle.dirft2d1([0.0], [0.0], [1.0], -1, 8, 6)
+    assert np.allclose(f, 1.0)
+    g = oracle.dirft3d1([0.0], [0.0], [0.0], [1.0], 1, 5, 4, 3)
+    assert np.allclose(g, 1.0)
+
+
+def test_mode_order_and_sign():
+    x, y = 0.3, -1.1
+    f = oracle.dirft2d1([x], [y], [1.0], -1, 6, 5)
+    for i in range(6):
+        for j in range(5):
+            k1, k2 = i - 3, j - 2
+            assert np.isclose(f[j, i], np.exp(-1j * (k1 * x + k2 * y)))
+    g = oracle.dirft2d1([x], [y], [1.0], +1, 6, 5)
+    assert np.allclose(g, np.conj(f))
+
+
+def test_perfect_lattice_bragg_peaks():
+    # 8x8 CELL lattice: x = 2pi*i/8 -> amplitude N at multiples of 8, 0 elsewhere
+    i, j = np.meshgrid(np.arange(8), np.arange(8), indexing="ij")
+    x = (2 * np.pi * i.ravel() / 8) - np.pi
+    y = (2 * np.pi * j.ravel() / 8) - np.pi
+    f = oracle.dirft2d1(x, y, np.ones(64), -1, 32, 32)
+    k = np.arange(32) - 16
+    peak = (k[:, None] % 8 == 0) & (k[None, :] % 8 == 0)
+    assert np.allclose(np.abs(f[peak]), 64)
+    assert np.max(np.abs(f[~peak])) < 1e-9
+
+
+def test_q_center_shift_equals_strength_phase():
+    rng = np.random.default_rng(3)
+    x, y = rng.uniform(-np.pi, np.pi, (2, 50))
+    c = np.exp(-1j * (2 * x + (-3) * y))  # shift by (2,-3) modes
+    f = oracle.dirft2d1(x, y, c, -1, 16, 16)
+    g = oracle.dirft2d1(x, y, np.ones(50), -1, 24, 24)
+    # f(k) = g(k + (2,-3))
+    assert np.allclose(f[8 - 8:16, :], g[12 - 8 - 3:12 + 8 - 3, 12 - 8 + 2:12 + 8 + 2])
+
+
+def test_3d_slices_equal_z_phased_2d():
+    # the mp_sql construction: slice kz of the 3D sum = 2D sum with strengths exp(-i kz z)
+    rng = np.random.default_rng(4)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 40))
+    f3 = oracle.dirft3d1(x, y, z, np.ones(40), -1, 10, 8, 6)
+    for l in range(6):
+        kz = l - 3
+        f2 = oracle.dirft2d1(x, y, np.exp(-1j * kz * z), -1, 10, 8)
+        assert np.allclose(f3[l], f2)
+
+
+@pytest.mark.parametrize("eps", [1e-6, 1e-9, 1e-12])
+def test_cpu_nufft_port_meets_tolerance_2d(eps):
+    rng = np.random.default_rng(5)
+    n = 3000
+    x, y = rng.uniform(-3 * np.pi, 3 * np.pi, (2, n))
+    c = rng.normal(size=n) + 1j * rng.normal(size=n)
+    ref = oracle.dirft2d1(x, y, c, -1, 48, 30)
+    got = oracle.es_nufft([x, y], c, -1, eps, (48, 30))
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 5 * eps
+
+
+def test_cpu_nufft_port_3d():
+    rng = np.random.default_rng(6)
+    n = 2000
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, n))
+    c = rng.normal(size=n) + 1j * rng.normal(size=n)
+    ref = oracle.dirft3d1(x, y, z, c, 1, 14, 12, 9)
+    got = oracle.es_nufft([x, y, z], c, 1, 1e-9, (14, 12, 9))
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_dirft_modes_matches_full_sum():
+    rng = np.random.default_rng(7)
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, 300))
+    c = rng.normal(size=300) + 0j
+    full = oracle.dirft3d1(x, y, z, c, -1, 8, 6, 4)
+    kq = np.array([[-4, -3, -2], [3, 2, 1], [0, 0, 0], [1, -1, 0]])
+    got = oracle.dirft_modes(x, y, z, c, -1, kq)
+    for q, (a, b, cc) in enumerate(kq):
+        assert np.isclose(got[q], full[cc + 2, b + 3, a + 4])
+
+
+def test_time_transforms_identities():
+    rng = np.random.default_rng(8)
+    F, nq = 40, 7
+    cs = rng.normal(size=(F, nq)) + 1j * rng.normal(size=(F, nq))
+    n_int = 21
+    w = sqom_ref.hann_window(n_int)
+    assert w[0] == 0 and np.isclose(w[n_int // 2], 1.0)
+    # E=const and dispersion give the same |X|^2 (the centring phase drops out)
+    for jf in (1, 4, 9):
+        e = sqom_ref.econst(cs, n_int, w, jf)
+        d = sqom_ref.dispersion(cs, n_int, w, np.arange(nq), 11)[:, jf - 1]
+        assert np.allclose(e, d)
+    # Parseval for a flat window over the full run
+    X = sqom_ref.dispersion(cs, F, np.ones(F), np.arange(nq), F)
+    x = sqom_ref.centered(cs)
+    assert np.allclose(X.sum(axis=1), F * (np.abs(x) ** 2).sum(axis=0))
+
+
+def test_single_exponential_peaks_at_its_bin():
+    F = 64
+    t = np.arange(F)
+    cs = np.exp(-2j * np.pi * 5 * t / F)[:, None] * np.ones((1, 3))
+    cs = cs + 0.0
+    s = sqom_ref.gauss_spectrum(cs, F / 2, F)
+    assert np.all(np.argmax(s, axis=0) == (-5) % F)
+    cs2 = np.exp(+2j * np.pi * 5 * t / F)[:, None] * np.ones((1, 3))
+    s2 = sqom_ref.gauss_spectrum(cs2, F / 2, F)
+    assert np.all(np.argmax(s2, axis=0) == 5)
