@@ -399,8 +399,33 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_profile_case(args):
+    """The per-frame pipeline of the benchmark job on a few frames only (for ncu captures:
+    same atoms, grid and kernels per frame; bounded device memory and launch count)."""
+    import torch
+
+    from mp_tools_gb300 import _lib
+    from mp_tools_gb300.sqom import SqomJob
+    global FRAMES
+    FRAMES = args.frames
+    pos0, counts, box, frames = make_workload(device="cuda")
+    grid = make_grid(box)
+    job = SqomJob(grid, species_counts=counts, n_frames=FRAMES, precision=_lib.FP32,
+                  stream=torch.cuda.current_stream().cuda_stream, **job_kwargs())
+    job.set_frames(frames)
+    for _ in range(2):
+        job.transform()
+    job.sync()
+    print(json.dumps({"profile_case": "ok", "frames": FRAMES, "modes": grid.n_q,
+                      "launches": int(_lib.load().mpsq_launch_count())}), flush=True)
+    job.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run the per-frame pipeline on --frames frames for profiler captures")
+    ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -410,7 +435,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
