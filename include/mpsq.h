@@ -215,6 +215,21 @@ int mpsq_job_sync(mpsq_job* job);
 int mpsq_job_profile(mpsq_job* job, int enable);
 int mpsq_job_stage_ms(mpsq_job* job, double* ms4, int64_t* frames, int reset);
 
+/* ---- allocation-free 2D type-1 transform -------------------------------------------
+ * No counterpart in the reference: an extra entry point of this library for callers that
+ * cannot allocate device memory during the call — code running while a CUDA graph is being
+ * captured, hosts whose device memory is owned by their own pool, plug-in hosts that forbid
+ * allocation.  Same transform and mode order as finufft2d1 (FP64), but every array is a
+ * DEVICE pointer and all scratch (fine grid, bins, point records) lives in a 16 MiB static
+ * device array that each GPU loading the library keeps until process exit.  Limits:
+ * nj <= 65536 points, ms, mt <= 256 modes; larger sizes return MPSQ_ERR_ARG.  Synchronous on
+ * `stream` (a cudaStream_t, NULL = default).  The first call on a device looks up the static
+ * array's address (once per device), so make it before any stream capture.  Calls that
+ * overlap on the GPU share the array and race: serialise them. */
+int mpsq_nufft2d1_noalloc(int64_t nj, const double* x, const double* y, const double* c,
+                          int iflag, double eps, int64_t ms, int64_t mt, double* fk,
+                          void* stream);
+
 /* ---- misc ----------------------------------------------------------------------------- */
 const char* mpsq_last_error(void);
 /* Library version string. */

@@ -28,6 +28,7 @@ EXPORTS = [
     "mpsq_job_set_cell_index", "mpsq_job_transform", "mpsq_job_amplitudes", "mpsq_job_sq_total",
     "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_gauss", "mpsq_job_sync",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_last_error", "mpsq_version", "mpsq_launch_count",
+    "mpsq_nufft2d1_noalloc",
 ]
 
 
@@ -117,6 +118,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_last_error": (C.c_char_p, []),
         "mpsq_version": (C.c_char_p, []),
         "mpsq_launch_count": (i64, []),
+        "mpsq_nufft2d1_noalloc": (C.c_int, [i64, vp, vp, vp, C.c_int, dbl, i64, i64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

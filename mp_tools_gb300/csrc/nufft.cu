@@ -398,6 +398,48 @@ __global__ void deconv_plan_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t
   fk[id] = v;
 }
 
+// In-place radix-2 FFT (length n = 2^logn <= 1024) along `qt` adjacent columns of a row-major
+// array with row stride `ld` (elements): column c of the CTA's tile is data[r*ld + col0 + c],
+// r = 0..n-1.  qt = 1 with ld = 1 and col0 = row*n transforms a contiguous row instead.
+// sign -1: exp(-2 pi i k t/n).  Used where no FFT library plan may be created.
+__global__ void fft_radix2_kernel(double2* __restrict__ data, int n, int logn, int64_t ld,
+                                  int64_t col_stride_blocks, int qt, int sign) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* xs = reinterpret_cast<double2*>(smem_raw);  // [n][qt]
+  double2* tw = xs + (size_t)n * qt;                   // [n/2]
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const int64_t base = (int64_t)blockIdx.x * col_stride_blocks;
+  for (int i = tid; i < n / 2; i += NT) {
+    double s_, c_;
+    sincospi((double)sign * 2.0 * (double)i / n, &s_, &c_);
+    tw[i] = make_double2(c_, s_);
+  }
+  for (int e = tid; e < n * qt; e += NT) {
+    const int r = e / qt, c = e % qt;
+    const int rr = (int)(__brev((unsigned)r) >> (32 - logn));
+    xs[rr * qt + c] = data[base + (int64_t)r * ld + c];
+  }
+  __syncthreads();
+  for (int s = 0; s < logn; ++s) {
+    const int half = 1 << s, stride = n >> (s + 1);
+    for (int e = tid; e < (n / 2) * qt; e += NT) {
+      const int c = e % qt, b = e / qt;
+      const int pos = b & (half - 1);
+      const int i = ((b >> s) << (s + 1)) + pos, j = i + half;
+      const double2 w = tw[pos * stride];
+      const double2 u = xs[i * qt + c], v0 = xs[j * qt + c];
+      const double2 v = make_double2(v0.x * w.x - v0.y * w.y, v0.x * w.y + v0.y * w.x);
+      xs[i * qt + c] = make_double2(u.x + v.x, u.y + v.y);
+      xs[j * qt + c] = make_double2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * qt; e += NT) {
+    const int r = e / qt, c = e % qt;
+    data[base + (int64_t)r * ld + c] = xs[r * qt + c];
+  }
+}
+
 // ------------------------------------------------------------------------- host helpers
 template <typename T>
 int launch_scan(const int* counts, int* starts, int64_t n, cudaStream_t s) {
@@ -710,3 +752,160 @@ extern "C" int mpsq_nufft_check_error(mpsq_nufft_plan* p) {
 extern "C" const char* mpsq_last_error(void) { return mpsq::t_err; }
 extern "C" const char* mpsq_version(void) { return "mpsq 0.1 (sm_103a)"; }
 extern "C" int64_t mpsq_launch_count(void) { return mpsq::g_launches.load(); }
+
+// ====================================================== allocation-free 2D type-1 entry point
+// For callers that may not allocate device memory (code running while a CUDA graph is being
+// captured, hosts whose device memory is handed out by their own pool, or plug-in hosts that
+// forbid allocation inside a call): all scratch of this transform — fine grid, bin counts and
+// offsets, point records, correction factors, error flag — lives in one file-scope device
+// array that every GPU loading this library holds until the process exits.
+namespace {
+
+constexpr int64_t kNoallocMaxPoints = 65536;   // nonuniform points per call
+constexpr int64_t kNoallocMaxModes = 256;      // modes per dimension
+constexpr int64_t kNoallocMaxFine = 512;       // fine grid per dimension (power of two)
+constexpr int kNoallocTile = 32;
+constexpr size_t kNoallocScratchBytes = size_t(16) << 20;  // 16 MiB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+std::mutex g_noalloc_mu;
+constexpr int kNoallocMaxDevices = 64;
+unsigned char* g_noalloc_base[kNoallocMaxDevices] = {};  // device address, per device ordinal
+
+constexpr size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+constexpr size_t noalloc_bytes(int64_t nf0, int64_t nf1, int64_t nj, int64_t ms, int64_t mt) {
+  return al256(sizeof(double2) * nf0 * nf1)                                    // fine grid
+         + 2 * al256(sizeof(int) * ((nf0 / kNoallocTile) * (nf1 / kNoallocTile) + 1))  // counts, starts
+         + al256(sizeof(mpsq::RecD) * 4 * (nj > 0 ? nj : 1))                    // records
+         + al256(sizeof(int) * 4 * (nj > 0 ? nj : 1))                           // source index
+         + al256(sizeof(double) * ms) + al256(sizeof(double) * mt) + al256(sizeof(double))
+         + al256(sizeof(int));                                                  // error flag
+}
+static_assert(noalloc_bytes(kNoallocMaxFine, kNoallocMaxFine, kNoallocMaxPoints, kNoallocMaxModes,
+                            kNoallocMaxModes) <= kNoallocScratchBytes,
+              "scratch array too small for the stated maximum sizes");
+
+int64_t pow2_at_least(int64_t n) {
+  int64_t p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+}  // namespace
+
+// Same transform as finufft2d1 (FP64, FINUFFT mode order) on DEVICE pointers, synchronous on
+// `stream`.  The first call on a device looks up the scratch array's device address (set-up,
+// done once per device with that device current), so that first call should come before any
+// stream capture.  Calls overlapping on the GPU (other host threads, other streams) race on
+// the shared scratch and must be serialised by the caller.
+extern "C" int mpsq_nufft2d1_noalloc(int64_t nj, const double* x, const double* y,
+                                     const double* c, int iflag, double eps, int64_t ms,
+                                     int64_t mt, double* fk, void* stream) {
+  using namespace mpsq;
+  if (nj < 0 || nj > kNoallocMaxPoints)
+    return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: nj = %lld outside 0..%lld (static scratch limit)",
+                (long long)nj, (long long)kNoallocMaxPoints);
+  if (ms < 1 || mt < 1 || ms > kNoallocMaxModes || mt > kNoallocMaxModes)
+    return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: modes %lld x %lld outside 1..%lld per dimension",
+                (long long)ms, (long long)mt, (long long)kNoallocMaxModes);
+  if (!fk || (nj > 0 && (!x || !y || !c)))
+    return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: null device pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  MPSQ_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices)
+    return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: device ordinal %d not supported", dev);
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return fail(MPSQ_ERR_CUDA, "nufft2d1_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+      g_noalloc_base[dev] = (unsigned char*)p;
+    }
+    base = g_noalloc_base[dev];
+  }
+  const EsKernel es = es_params(eps, MPSQ_FP64);
+  const int64_t nf0 = std::max<int64_t>(kNoallocTile, pow2_at_least(std::max<int64_t>(2 * ms, 2 * es.w)));
+  const int64_t nf1 = std::max<int64_t>(kNoallocTile, pow2_at_least(std::max<int64_t>(2 * mt, 2 * es.w)));
+  if (nf0 > kNoallocMaxFine || nf1 > kNoallocMaxFine ||
+      noalloc_bytes(nf0, nf1, nj, ms, mt) > kNoallocScratchBytes)
+    return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: problem exceeds the static scratch");
+  SpreadArgs a{};
+  a.dim = 2;
+  a.w = es.w;
+  a.beta = es.beta;
+  a.nf[0] = nf0;
+  a.nf[1] = nf1;
+  a.nf[2] = 1;
+  a.tile[0] = a.tile[1] = kNoallocTile;
+  a.tile[2] = 1;
+  a.ntile[0] = (int)(nf0 / kNoallocTile);
+  a.ntile[1] = (int)(nf1 / kNoallocTile);
+  a.ntile[2] = 1;
+  a.n_tiles = (int64_t)a.ntile[0] * a.ntile[1];
+  a.n_fine = nf0 * nf1;
+  a.ngrid = 1;
+  const int64_t cap = 4 * std::max<int64_t>(nj, 1);
+  // carve the scratch array
+  unsigned char* q = base;
+  auto take = [&](size_t bytes) {
+    unsigned char* r = q;
+    q += al256(bytes);
+    return r;
+  };
+  double2* fine = (double2*)take(sizeof(double2) * a.n_fine);
+  int* counts = (int*)take(sizeof(int) * (a.n_tiles + 1));
+  int* starts = (int*)take(sizeof(int) * (a.n_tiles + 1));
+  RecD* recs = (RecD*)take(sizeof(RecD) * cap);
+  int* idx = (int*)take(sizeof(int) * cap);
+  double* corr0 = (double*)take(sizeof(double) * ms);
+  double* corr1 = (double*)take(sizeof(double) * mt);
+  double* corr2 = (double*)take(sizeof(double));
+  int* err = (int*)take(sizeof(int));
+  // deconvolution factors (host quadrature, copied into the scratch)
+  std::vector<double> h0(ms), h1(mt);
+  const double one = 1.0;
+  es_correction(es, nf0, ms, h0.data());
+  es_correction(es, nf1, mt, h1.data());
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr0, h0.data(), sizeof(double) * ms, cudaMemcpyHostToDevice, s));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr1, h1.data(), sizeof(double) * mt, cudaMemcpyHostToDevice, s));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr2, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+  // the previous call's contents stay in the array: clear what must start at zero
+  MPSQ_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (a.n_tiles + 1), s));
+  const int bt = 256;
+  const unsigned nb = (unsigned)std::max<int64_t>(1, (nj + bt - 1) / bt);
+  if (nj > 0) {
+    bin_plan_kernel<double><<<nb, bt, 0, s>>>(nj, x, y, nullptr, a, 0, counts, starts, recs, idx, cap, err);
+    MPSQ_LAUNCH_CHECK();
+  }
+  int rc = launch_scan<double>(counts, starts, a.n_tiles, s);
+  if (rc) return rc;
+  MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (a.n_tiles + 1), s));
+  if (nj > 0) {
+    bin_plan_kernel<double><<<nb, bt, 0, s>>>(nj, x, y, nullptr, a, 1, counts, starts, recs, idx, cap, err);
+    MPSQ_LAUNCH_CHECK();
+  }
+  rc = launch_spread_impl<double, 2, 128>(a, recs, idx, (const double2*)c, nj, starts,
+                                          (int)a.n_tiles, 1, false, fine, s);
+  if (rc) return rc;
+  const int sign = iflag >= 0 ? 1 : -1;
+  int l0 = 0, l1 = 0;
+  while ((int64_t(1) << l0) < nf0) ++l0;
+  while ((int64_t(1) << l1) < nf1) ++l1;
+  // rows (length nf0, contiguous), then columns (length nf1, stride nf0), 4 columns per CTA
+  fft_radix2_kernel<<<(unsigned)nf1, 256, sizeof(double2) * (nf0 + nf0 / 2), s>>>(fine, (int)nf0, l0, 1, nf0, 1, sign);
+  MPSQ_LAUNCH_CHECK();
+  fft_radix2_kernel<<<(unsigned)(nf0 / 4), 256, sizeof(double2) * (nf1 * 4 + nf1 / 2), s>>>(fine, (int)nf1, l1, nf0, 4, 4, sign);
+  MPSQ_LAUNCH_CHECK();
+  const int64_t nm = ms * mt;
+  deconv_plan_kernel<double><<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(
+      a, ms, mt, 1, fine, corr0, corr1, corr2, (double2*)fk, 1);
+  MPSQ_LAUNCH_CHECK();
+  return check_dev_error(err, s);
+}
