@@ -413,10 +413,14 @@ def run_profile_case(args):
     job = SqomJob(grid, species_counts=counts, n_frames=FRAMES, precision=_lib.FP32,
                   stream=torch.cuda.current_stream().cuda_stream, **job_kwargs())
     job.set_frames(frames)
-    for _ in range(2):
-        job.transform()
+    job.transform()
+    job.profile(True)
+    job.transform()
     job.sync()
+    st, nfr = job.stage_ms()
     print(json.dumps({"profile_case": "ok", "frames": FRAMES, "modes": grid.n_q,
+                      "stage_ms_per_frame": dict(zip(["bin", "spread", "fft", "deconv"],
+                                                     [s / max(nfr, 1) for s in st])),
                       "launches": int(_lib.load().mpsq_launch_count())}), flush=True)
     job.close()
 

@@ -43,6 +43,12 @@ struct PrepArgs {
   int window;
   int pack;
   int64_t n_atoms_frame;
+  // FP32 path: fine-grid coordinate g_k = sum_b A_kb r_b + B_k as hi+lo float pairs, and the
+  // strength phase in turns q_center . r likewise
+  float ahi[3][3], alo[3][3], bhi[3], blo[3];
+  float qhi[3], qlo[3];
+  float inv_nf[3];
+  int nf[3];
 };
 
 // Parameters of the fused deconvolution / weighting.
@@ -61,6 +67,33 @@ struct WeightArgs {
   double wnorm;
   int store_species;
   int n_species;
+  // FP32 copies (the FP32 path must not convert from double per element: FP64 pipe)
+  float b_coh_f[MPSQ_MAX_SPECIES];
+  float xff_f[MPSQ_MAX_SPECIES][9];
+  float kappa_f, q0_f[3], qs_f[3][3], extra_f, wnorm_f;
+};
+
+template <typename T>
+struct WP;  // typed views of WeightArgs
+template <>
+struct WP<float> {
+  static __device__ __forceinline__ float b(const WeightArgs& w, int s) { return w.b_coh_f[s]; }
+  static __device__ __forceinline__ float x(const WeightArgs& w, int s, int i) { return w.xff_f[s][i]; }
+  static __device__ __forceinline__ float kappa(const WeightArgs& w) { return w.kappa_f; }
+  static __device__ __forceinline__ float q0(const WeightArgs& w, int b) { return w.q0_f[b]; }
+  static __device__ __forceinline__ float qs(const WeightArgs& w, int k, int b) { return w.qs_f[k][b]; }
+  static __device__ __forceinline__ float extra(const WeightArgs& w) { return w.extra_f; }
+  static __device__ __forceinline__ float wnorm(const WeightArgs& w) { return w.wnorm_f; }
+};
+template <>
+struct WP<double> {
+  static __device__ __forceinline__ double b(const WeightArgs& w, int s) { return w.b_coh[s]; }
+  static __device__ __forceinline__ double x(const WeightArgs& w, int s, int i) { return w.xff[s][i]; }
+  static __device__ __forceinline__ double kappa(const WeightArgs& w) { return w.kappa; }
+  static __device__ __forceinline__ double q0(const WeightArgs& w, int b) { return w.q0[b]; }
+  static __device__ __forceinline__ double qs(const WeightArgs& w, int k, int b) { return w.qs[k][b]; }
+  static __device__ __forceinline__ double extra(const WeightArgs& w) { return w.extra_sq; }
+  static __device__ __forceinline__ double wnorm(const WeightArgs& w) { return w.wnorm; }
 };
 
 }  // namespace mpsq
@@ -98,67 +131,6 @@ struct mpsq_job {
 
 namespace mpsq {
 
-__device__ __forceinline__ double to_grid_j(double x, double nf) {
-  double g = x * (nf * 0.15915494309189533576888376337251436);
-  g -= nf * floor(g / nf);
-  if (g >= nf) g -= nf;
-  if (!(g >= 0.0 && g < nf)) g = 0.0;  // NaN / inf coordinates: keep every index in range
-  return g;
-}
-
-// Same halo-copy emission as the plan API (kept local to this unit so it inlines).
-template <typename T>
-__device__ __forceinline__ void emit_job(const SpreadArgs& a, const double g[3], int keygrid,
-                                         int comp, bool scatter, int* cursor,
-                                         const int* starts, typename RecOf<T>::type* recs,
-                                         typename Cplx<T>::type* str_out,
-                                         typename Cplx<T>::type strength, int64_t cap,
-                                         int* err) {
-  int64_t i0[3], tlo[3], thi[3];
-  T d[3];
-  for (int k = 0; k < 3; ++k) {
-    if (k < a.dim) {
-      const int64_t s = (int64_t)ceil(g[k] - 0.5 * a.w);
-      i0[k] = s;
-      d[k] = (T)((double)s - g[k]);
-      tlo[k] = s >= 0 ? s / a.tile[k] : -((-s + a.tile[k] - 1) / a.tile[k]);
-      const int64_t e = s + a.w - 1;
-      thi[k] = e >= 0 ? e / a.tile[k] : -((-e + a.tile[k] - 1) / a.tile[k]);
-    } else {
-      i0[k] = 0;
-      d[k] = (T)0;
-      tlo[k] = thi[k] = 0;
-    }
-  }
-  for (int64_t tz = tlo[2]; tz <= thi[2]; ++tz) {
-    const int64_t wz = ((tz % a.ntile[2]) + a.ntile[2]) % a.ntile[2];
-    const int lz = (int)(i0[2] - tz * a.tile[2]);
-    for (int64_t ty = tlo[1]; ty <= thi[1]; ++ty) {
-      const int64_t wy = ((ty % a.ntile[1]) + a.ntile[1]) % a.ntile[1];
-      const int ly = (int)(i0[1] - ty * a.tile[1]);
-      for (int64_t tx = tlo[0]; tx <= thi[0]; ++tx) {
-        const int64_t wx = ((tx % a.ntile[0]) + a.ntile[0]) % a.ntile[0];
-        const int lx = (int)(i0[0] - tx * a.tile[0]);
-        const int64_t key = (int64_t)keygrid * a.n_tiles + (wz * a.ntile[1] + wy) * a.ntile[0] + wx;
-        const int slot = atomicAdd(&cursor[key], 1);
-        if (!scatter) continue;
-        const int64_t pos = (int64_t)starts[key] + slot;
-        if (pos >= (int64_t)starts[key + 1] || pos >= cap) {
-          atomicOr(err, kErrRecOverflow);
-          continue;
-        }
-        typename RecOf<T>::type r;
-        r.dx = d[0];
-        r.dy = d[1];
-        r.dz = d[2];
-        r.packed = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
-        recs[pos] = r;
-        str_out[pos] = strength;
-      }
-    }
-  }
-}
-
 // Selection, phases and strengths of one atom of one frame (mp_sqom56.f90:1104-1142), then
 // binning.  Pass 0 counts, pass 1 scatters.
 template <typename T>
@@ -181,13 +153,50 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
       const int c3[3] = {ci.x, ci.y, ci.z};
       for (int k = 0; k < 3; ++k) {
         const int c = c3[k] - p.n_row[k] / 2 - 1;
-        if ((double)c < p.pos_min[k] || (double)c > p.pos_max[k]) return;  // (:1109-1111)
+        if ((float)c < p.pos_min_f[k] || (float)c > p.pos_max_f[k]) return;  // (:1109-1111)
       }
     }
   } else {
     const float rr[3] = {r.x, r.y, r.z};
     for (int k = 0; k < 3; ++k)  // (:1121-1128)
       if (!(rr[k] >= p.pos_min_f[k] - p.tol_f && rr[k] < p.pos_max_f[k] + p.tol_f)) return;
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (!p.phase_rounding) {
+      // FP32 split precision: exact phase reduction in two-float arithmetic (no FP64 pipe)
+      const float rf[3] = {r.x, r.y, r.z};
+      int sc[3] = {0, 0, 0};
+      float dc[3] = {0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < p.dim; ++k) {
+        const F2 gk = affine_f2(rf, p.ahi[k], p.alo[k], p.bhi[k], p.blo[k]);
+        split_cell_f2(gk, p.nf[k], p.inv_nf[k], a.w, &sc[k], &dc[k]);
+      }
+      float2 c = make_float2(1.0f, 0.0f);
+      if (p.has_qc) {
+        const F2 t = affine_f2(rf, p.qhi, p.qlo, 0.0f, 0.0f);
+        const float fl = floorf(t.hi);
+        const float fr = __fadd_rn(__fsub_rn(t.hi, fl), t.lo);
+        float sn, cn;
+        sincospif(2.0f * fr, &sn, &cn);
+        c = make_float2(cn, -sn);
+      }
+      if (p.window) {  // spatial Hann window (1+cos x)(1+cos y) (:1118)
+        const int nw = p.dim == 2 ? 2 : 3;
+        float f = 1.0f;
+        for (int k = 0; k < nw; ++k) {
+          float pr = 0.0f;
+          for (int b = 0; b < 3; ++b) pr = fmaf(p.axis_f[k][b], rf[b] - p.centre_f[b], pr);
+          f *= 1.0f + cosf(pr * p.tpe_f[k]);
+        }
+        c.x *= f;
+        c.y *= f;
+      }
+      const int comp = p.pack ? p.comp_of[s] : 0;
+      if (p.pack && c.x == 0.0f) return;
+      emit_cells<float>(a, sc, dc, grid, comp, scatter != 0, cursor, starts, (RecF*)recs,
+                        (float2*)str, c, nullptr, 0, cap, err);
+      return;
+    }
   }
   double x[3] = {0.0, 0.0, 0.0};
   double g[3] = {0.0, 0.0, 0.0};
@@ -204,7 +213,7 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
       for (int b = 0; b < 3; ++b) pr += p.axis[k][b] * (rd[b] - p.centre[b]);
       x[k] = pr * p.tpe[k];
     }
-    g[k] = to_grid_j(x[k], (double)a.nf[k]);
+    g[k] = fold_grid(x[k] * a.gscale[k], (double)a.nf[k], a.ginv[k]);
   }
   typename Cplx<T>::type c;
   if (p.has_qc) {
@@ -253,44 +262,52 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
   }
   const int comp = p.pack ? p.comp_of[s] : 0;
   if (p.pack && c.x == (T)0) return;  // zero strength contributes nothing
-  emit_job<T>(a, g, grid, comp, scatter != 0, cursor, starts, recs, str, c, cap, err);
+  emit_records<T>(a, g, grid, comp, scatter != 0, cursor, starts, recs, str, c, nullptr, 0, cap,
+                  err);
 }
 
 template <typename T>
 __device__ __forceinline__ T species_weight(const WeightArgs& w, int s, T s2) {
-  if (w.weight_mode == MPSQ_WEIGHT_NEUTRON) return (T)w.b_coh[s];
+  if (w.weight_mode == MPSQ_WEIGHT_NEUTRON) return WP<T>::b(w, s);
   if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
-    T f = (T)w.xff[s][8];
-    for (int i = 0; i < 4; ++i) f += (T)w.xff[s][2 * i] * exp(-(T)w.xff[s][2 * i + 1] * s2);
+    T f = WP<T>::x(w, s, 8);
+    for (int i = 0; i < 4; ++i) f += WP<T>::x(w, s, 2 * i) * exp(-WP<T>::x(w, s, 2 * i + 1) * s2);
     return f;
   }
   return (T)1;
 }
 
 // Deconvolution, pair separation, species weighting; writes cs(t, Q) for one frame.
+// Grid: x over the m0 modes of a row, y over the m1*m2 rows (32-bit index math).
 template <typename T>
-__global__ void job_deconv_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t m2,
+__global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
                                   const typename Cplx<T>::type* __restrict__ fine,
                                   const T* __restrict__ c0, const T* __restrict__ c1,
                                   const T* __restrict__ c2, WeightArgs w,
                                   typename Cplx<T>::type* __restrict__ cs_frame,
                                   typename Cplx<T>::type* __restrict__ cs_species_frame) {
   using C = typename Cplx<T>::type;
-  const int64_t nm = m0 * m1 * m2;
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nm) return;
-  const int64_t i = q % m0, j = (q / m0) % m1, l = q / (m0 * m1);
-  const int64_t kx = i - m0 / 2, ky = j - m1 / 2, kz = l - m2 / 2;
-  const int64_t nf0 = a.nf[0], nf1 = a.nf[1], nf2 = a.nf[2];
-  const int64_t src = (((kz + nf2) % nf2) * nf1 + ((ky + nf1) % nf1)) * nf0 + ((kx + nf0) % nf0);
-  const int64_t srcm = (((nf2 - kz) % nf2) * nf1 + ((nf1 - ky) % nf1)) * nf0 + ((nf0 - kx) % nf0);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m0) return;
+  const int j = blockIdx.y, l = blockIdx.z;
+  const int row = l * m1 + j;
+  const int64_t nm = (int64_t)m0 * m1 * m2;
+  const int64_t q = (int64_t)row * m0 + i;
+  const int kx = i - m0 / 2, ky = j - m1 / 2, kz = l - m2 / 2;
+  const int nf0 = (int)a.nf[0], nf1 = (int)a.nf[1], nf2 = (int)a.nf[2];
+  // fine-grid positions of mode k and of -k (periodic)
+  const int sx = kx < 0 ? kx + nf0 : kx, sy = ky < 0 ? ky + nf1 : ky, sz = kz < 0 ? kz + nf2 : kz;
+  const int mx = kx > 0 ? nf0 - kx : -kx, my = ky > 0 ? nf1 - ky : -ky, mz = kz > 0 ? nf2 - kz : -kz;
+  const int64_t src = ((int64_t)sz * nf1 + sy) * nf0 + sx;
+  const int64_t srcm = ((int64_t)mz * nf1 + my) * nf0 + mx;
   const T corr = c0[i] * c1[j] * c2[l];
   T s2 = 0;
   if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
     T qv[3];
     for (int b = 0; b < 3; ++b)
-      qv[b] = (T)w.q0[b] + (T)kx * (T)w.qs[0][b] + (T)ky * (T)w.qs[1][b] + (T)kz * (T)w.qs[2][b];
-    s2 = (T)w.kappa * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + (T)w.extra_sq);
+      qv[b] = WP<T>::q0(w, b) + (T)kx * WP<T>::qs(w, 0, b) + (T)ky * WP<T>::qs(w, 1, b) +
+              (T)kz * WP<T>::qs(w, 2, b);
+    s2 = WP<T>::kappa(w) * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + WP<T>::extra(w));
   }
   T accr = 0, acci = 0;
   for (int gi = 0; gi < w.ngroups; ++gi) {
@@ -305,10 +322,10 @@ __global__ void job_deconv_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t 
       acci += wa * ai + wb * bi;
       if (w.store_species) {
         C va, vb;
-        va.x = ar * (T)w.wnorm;
-        va.y = ai * (T)w.wnorm;
-        vb.x = br * (T)w.wnorm;
-        vb.y = bi * (T)w.wnorm;
+        va.x = ar * WP<T>::wnorm(w);
+        va.y = ai * WP<T>::wnorm(w);
+        vb.x = br * WP<T>::wnorm(w);
+        vb.y = bi * WP<T>::wnorm(w);
         cs_species_frame[(int64_t)sa * nm + q] = va;
         cs_species_frame[(int64_t)sb * nm + q] = vb;
       }
@@ -319,15 +336,15 @@ __global__ void job_deconv_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t 
       acci += wa * G.y * corr;
       if (w.store_species) {
         C va;
-        va.x = G.x * corr * (T)w.wnorm;
-        va.y = G.y * corr * (T)w.wnorm;
+        va.x = G.x * corr * WP<T>::wnorm(w);
+        va.y = G.y * corr * WP<T>::wnorm(w);
         cs_species_frame[(int64_t)sa * nm + q] = va;
       }
     }
   }
   C out;
-  out.x = accr * (T)w.wnorm;
-  out.y = acci * (T)w.wnorm;
+  out.x = accr * WP<T>::wnorm(w);
+  out.y = acci * WP<T>::wnorm(w);
   cs_frame[q] = out;
 }
 
@@ -451,6 +468,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   a.n_tiles = j->g.n_tiles;
   a.n_fine = j->g.n_fine;
   a.ngrid = std::max(1, j->ngroups);
+  finish_spread_args(a);
   // preparation parameters
   PrepArgs& p = j->pa;
   p.dim = d->ndim;
@@ -486,6 +504,22 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   p.window = d->spatial_window;
   p.pack = pack;
   p.n_atoms_frame = d->n_atoms_frame;
+  for (int k = 0; k < 3; ++k) {
+    const double sc = d->tpe[k] * a.gscale[k];  // radians -> fine-grid units along axis k
+    double bk = 0.0;
+    for (int b = 0; b < 3; ++b) {
+      const double A = d->axis[k][b] * sc;
+      p.ahi[k][b] = (float)A;
+      p.alo[k][b] = (float)(A - (double)p.ahi[k][b]);
+      bk -= A * d->centre[b];
+    }
+    p.bhi[k] = (float)bk;
+    p.blo[k] = (float)(bk - (double)p.bhi[k]);
+    p.qhi[k] = (float)d->q_center[k];
+    p.qlo[k] = (float)(d->q_center[k] - (double)p.qhi[k]);
+    p.nf[k] = (int)j->g.nf[k];
+    p.inv_nf[k] = (float)(1.0 / (double)j->g.nf[k]);
+  }
   // weighting parameters
   WeightArgs& w = j->wa;
   w.ngroups = j->ngroups;
@@ -506,6 +540,17 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   }
   w.extra_sq = d->qphys_extra_sq;
   w.wnorm = d->spatial_window ? (d->ndim == 2 ? 0.25 : 0.125) : 1.0;
+  for (int s = 0; s < d->n_species; ++s) {
+    w.b_coh_f[s] = (float)w.b_coh[s];
+    for (int i = 0; i < 9; ++i) w.xff_f[s][i] = (float)w.xff[s][i];
+  }
+  w.kappa_f = (float)w.kappa;
+  for (int b = 0; b < 3; ++b) {
+    w.q0_f[b] = (float)w.q0[b];
+    for (int k = 0; k < 3; ++k) w.qs_f[k][b] = (float)w.qs[k][b];
+  }
+  w.extra_f = (float)w.extra_sq;
+  w.wnorm_f = (float)w.wnorm;
   w.store_species = d->store_species;
   w.n_species = d->n_species;
 
@@ -628,8 +673,9 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     if (mark(3)) return MPSQ_ERR_CUDA;
     C* csf = (C*)j->cs + (size_t)t * nm;
     C* css = j->cs_species ? (C*)j->cs_species + (size_t)t * j->d.n_species * nm : nullptr;
-    job_deconv_kernel<T><<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(
-        a, j->g.m[0], j->g.m[1], j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
+    const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1], (unsigned)j->g.m[2]);
+    job_deconv_kernel<T><<<dgrid, 128, 0, s>>>(
+        a, (int)j->g.m[0], (int)j->g.m[1], (int)j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
         (const T*)j->corr[1], (const T*)j->corr[2], j->wa, csf, css);
     MPSQ_LAUNCH_CHECK();
     if (prof) {

@@ -106,7 +106,173 @@ struct SpreadArgs {
   int64_t n_tiles;
   int64_t n_fine;
   int ngrid;
+  double gscale[3];  // nf / (2 pi): radians -> fine-grid units
+  double ginv[3];    // 1 / nf
 };
+
+inline void finish_spread_args(SpreadArgs& a) {
+  for (int k = 0; k < 3; ++k) {
+    a.gscale[k] = (double)a.nf[k] * 0.15915494309189533576888376337251436;
+    a.ginv[k] = 1.0 / (double)a.nf[k];
+  }
+}
+
+// Fold a fine-grid coordinate into [0, nf); NaN / inf give 0 so every index stays in range.
+__device__ __forceinline__ double fold_grid(double g, double nf, double inv_nf) {
+  g -= nf * floor(g * inv_nf);
+  if (g >= nf) g -= nf;
+  if (g < 0.0) g += nf;
+  if (!(g >= 0.0 && g < nf)) g = 0.0;
+  return g;
+}
+
+// ---- exact phase reduction in FP32 arithmetic (Dekker product, Knuth sum)
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+// sum_b r_b (A_hi[b] + A_lo[b]) + (B_hi + B_lo) with ~45-bit accuracy: each product r*A_hi is
+// split exactly with an FMA, the hi parts are summed exactly, the small parts in FP32.
+__device__ __forceinline__ F2 affine_f2(const float r[3], const float* ahi, const float* alo,
+                                        float bhi, float blo) {
+  float hi = bhi, lo = blo;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const float p = __fmul_rn(r[b], ahi[b]);
+    const float pe = fmaf(r[b], ahi[b], -p);
+    const F2 s = two_sum(hi, p);
+    hi = s.hi;
+    lo = __fadd_rn(lo, __fadd_rn(s.lo, fmaf(r[b], alo[b], pe)));
+  }
+  const F2 s = two_sum(hi, lo);
+  return s;
+}
+// Folds g = hi + lo into [0, nf) and returns the first support cell s = ceil(g - w/2) and the
+// offset d = s - g in [-w/2, -w/2 + 1), both exact up to the FP32 rounding of d.
+__device__ __forceinline__ void split_cell_f2(F2 g, int nf, float inv_nf, int w, int* s, float* d) {
+  const float fnf = (float)nf;
+  const float n = floorf(__fmul_rn(g.hi, inv_nf));
+  // remove the integer multiple of nf keeping the result as a hi+lo pair (the shifted value
+  // can be larger than g.hi, so a plain FP32 subtraction would round)
+  F2 t = two_sum(g.hi, -__fmul_rn(n, fnf));
+  t = two_sum(t.hi, __fadd_rn(t.lo, g.lo));
+  float gh = t.hi, gl = t.lo;
+  if (!(gh == gh) || !(gl == gl) || fabsf(gh) > 4.0f * fnf) {  // NaN / inf input
+    gh = 0.0f;
+    gl = 0.0f;
+  }
+  if (__fadd_rn(gh, gl) < 0.0f) {
+    t = two_sum(gh, fnf);
+    gh = t.hi;
+    gl = __fadd_rn(gl, t.lo);
+  }
+  if (__fadd_rn(gh, gl) >= fnf) {
+    t = two_sum(gh, -fnf);
+    gh = t.hi;
+    gl = __fadd_rn(gl, t.lo);
+  }
+  const float hw = 0.5f * (float)w;
+  float c = ceilf(__fsub_rn(gh, hw));
+  float dd = __fsub_rn(__fsub_rn(c, gh), gl);  // c - gh is exact (integer minus nearby float)
+  if (dd < -hw) {
+    c += 1.0f;
+    dd = __fadd_rn(dd, 1.0f);
+  } else if (dd >= 1.0f - hw) {
+    c -= 1.0f;
+    dd = __fsub_rn(dd, 1.0f);
+  }
+  int si = (int)c;
+  // keep the first cell in [-w/2 - 1, nf) whatever the input
+  si = si < -w ? -w : (si >= nf ? nf - 1 : si);
+  *s = si;
+  *d = dd;
+}
+
+// Emits the halo copies of one point whose support starts at cell s[k] with offset d[k]:
+// one record per tile its w-cell support touches (at most 2 per dimension, periodic).
+// Pass 0 (scatter = false) counts records per (grid, tile) key into `cursor`; pass 1 writes
+// them at starts[key] + slot, `cursor` having been zeroed between the passes.
+template <typename T>
+__device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3], const T d_in[3],
+                                           int keygrid, int comp, bool scatter, int* cursor,
+                                           const int* __restrict__ starts,
+                                           typename RecOf<T>::type* recs,
+                                           typename Cplx<T>::type* str_out,
+                                           typename Cplx<T>::type strength, int* idx_out,
+                                           int src_index, int64_t cap, int* err) {
+  int i0[3], tlo[3], thi[3];
+  T d[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k < a.dim) {
+      const int s = s_in[k];        // first cell of the support
+      const int e = s + a.w - 1;    // last cell
+      const int t = a.tile[k];
+      i0[k] = s;
+      d[k] = d_in[k];
+      tlo[k] = s >= 0 ? s / t : -((t - 1 - s) / t);   // >= -1 since s >= -w and t >= w
+      thi[k] = e >= 0 ? e / t : -((t - 1 - e) / t);   // <= ntile since e < nf + t
+    } else {
+      i0[k] = 0;
+      d[k] = (T)0;
+      tlo[k] = thi[k] = 0;
+    }
+  }
+  for (int tz = tlo[2]; tz <= thi[2]; ++tz) {
+    const int wz = tz < 0 ? tz + a.ntile[2] : (tz >= a.ntile[2] ? tz - a.ntile[2] : tz);
+    const int lz = i0[2] - tz * a.tile[2];
+    for (int ty = tlo[1]; ty <= thi[1]; ++ty) {
+      const int wy = ty < 0 ? ty + a.ntile[1] : (ty >= a.ntile[1] ? ty - a.ntile[1] : ty);
+      const int ly = i0[1] - ty * a.tile[1];
+      for (int tx = tlo[0]; tx <= thi[0]; ++tx) {
+        const int wx = tx < 0 ? tx + a.ntile[0] : (tx >= a.ntile[0] ? tx - a.ntile[0] : tx);
+        const int lx = i0[0] - tx * a.tile[0];
+        const int64_t key = (int64_t)keygrid * a.n_tiles + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx;
+        const int slot = atomicAdd(&cursor[key], 1);
+        if (!scatter) continue;
+        const int64_t pos = (int64_t)starts[key] + slot;
+        if (pos >= (int64_t)starts[key + 1] || pos >= cap) {
+          atomicOr(err, 1);
+          continue;
+        }
+        typename RecOf<T>::type r;
+        r.dx = d[0];
+        r.dy = d[1];
+        r.dz = d[2];
+        r.packed = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
+        recs[pos] = r;
+        if (str_out) str_out[pos] = strength;
+        if (idx_out) idx_out[pos] = src_index;
+      }
+    }
+  }
+}
+
+// Same from a folded FP64 fine-grid coordinate g (the FP64 path and the plan API).
+template <typename T>
+__device__ __forceinline__ void emit_records(const SpreadArgs& a, const double g[3], int keygrid,
+                                             int comp, bool scatter, int* cursor,
+                                             const int* __restrict__ starts,
+                                             typename RecOf<T>::type* recs,
+                                             typename Cplx<T>::type* str_out,
+                                             typename Cplx<T>::type strength, int* idx_out,
+                                             int src_index, int64_t cap, int* err) {
+  int s[3] = {0, 0, 0};
+  T d[3] = {(T)0, (T)0, (T)0};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (k < a.dim) {
+      s[k] = (int)ceil(g[k] - 0.5 * a.w);
+      d[k] = (T)((double)s[k] - g[k]);
+    }
+  emit_cells<T>(a, s, d, keygrid, comp, scatter, cursor, starts, recs, str_out, strength, idx_out,
+                src_index, cap, err);
+}
 
 // ------------------------------------------------------------------ shared kernel helpers
 // Launch helpers implemented in nufft.cu, used by the plan API and the job pipeline.

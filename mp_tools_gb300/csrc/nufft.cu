@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -149,75 +150,6 @@ int check_dev_error(const int* dev_flag, cudaStream_t s) {
 }
 
 // --------------------------------------------------------------------------- device code
-__device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {
-  return a >= 0 ? a / b : -((-a + b - 1) / b);
-}
-
-// Fold a coordinate in radians to a fine-grid coordinate in [0, nf).
-__device__ __forceinline__ double to_grid(double x, double nf) {
-  double g = x * (nf * 0.15915494309189533576888376337251436);  // nf / (2 pi)
-  g -= nf * floor(g / nf);
-  if (g >= nf) g -= nf;
-  if (!(g >= 0.0 && g < nf)) g = 0.0;  // NaN / inf coordinates: keep every index in range
-  return g;
-}
-
-// Emits the halo copies of one point.  Pass 0 counts records per (grid, tile) key; pass 1
-// writes them, using `cursor` (zeroed between the passes) for the slot within the key.
-template <typename T>
-__device__ __forceinline__ void emit_point(const SpreadArgs& a, const double g[3], int keygrid,
-                                           int comp, bool scatter, int* cursor,
-                                           const int* starts, typename RecOf<T>::type* recs,
-                                           typename Cplx<T>::type* str_out,
-                                           typename Cplx<T>::type strength, int* idx_out,
-                                           int src_index, int64_t cap, int* err) {
-  int64_t i0[3];
-  int64_t tlo[3], thi[3];
-  T d[3];
-  for (int k = 0; k < 3; ++k) {
-    if (k < a.dim) {
-      double h = g[k] - 0.5 * a.w;
-      int64_t s = (int64_t)ceil(h);
-      i0[k] = s;
-      d[k] = (T)((double)s - g[k]);
-      tlo[k] = floor_div(s, a.tile[k]);
-      thi[k] = floor_div(s + a.w - 1, a.tile[k]);
-    } else {
-      i0[k] = 0;
-      d[k] = (T)0;
-      tlo[k] = thi[k] = 0;
-    }
-  }
-  for (int64_t tz = tlo[2]; tz <= thi[2]; ++tz) {
-    int64_t wz = ((tz % a.ntile[2]) + a.ntile[2]) % a.ntile[2];
-    int lz = (int)(i0[2] - tz * a.tile[2]);
-    for (int64_t ty = tlo[1]; ty <= thi[1]; ++ty) {
-      int64_t wy = ((ty % a.ntile[1]) + a.ntile[1]) % a.ntile[1];
-      int ly = (int)(i0[1] - ty * a.tile[1]);
-      for (int64_t tx = tlo[0]; tx <= thi[0]; ++tx) {
-        int64_t wx = ((tx % a.ntile[0]) + a.ntile[0]) % a.ntile[0];
-        int lx = (int)(i0[0] - tx * a.tile[0]);
-        int64_t key = (int64_t)keygrid * a.n_tiles + (wz * a.ntile[1] + wy) * a.ntile[0] + wx;
-        int slot = atomicAdd(&cursor[key], 1);
-        if (!scatter) continue;
-        int64_t pos = (int64_t)starts[key] + slot;
-        if (pos >= (int64_t)starts[key + 1] || pos >= cap) {
-          atomicOr(err, kErrRecOverflow);
-          continue;
-        }
-        typename RecOf<T>::type r;
-        r.dx = d[0];
-        r.dy = d[1];
-        r.dz = d[2];
-        r.packed = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
-        recs[pos] = r;
-        if (str_out) str_out[pos] = strength;
-        if (idx_out) idx_out[pos] = src_index;
-      }
-    }
-  }
-}
-
 // Plan API binning: coordinates in radians (FINUFFT convention).
 template <typename T>
 __global__ void bin_plan_kernel(int64_t nj, const T* __restrict__ x, const T* __restrict__ y,
@@ -228,14 +160,14 @@ __global__ void bin_plan_kernel(int64_t nj, const T* __restrict__ x, const T* __
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nj) return;
   double g[3] = {0.0, 0.0, 0.0};
-  g[0] = to_grid((double)x[j], (double)a.nf[0]);
-  g[1] = to_grid((double)y[j], (double)a.nf[1]);
-  if (a.dim == 3) g[2] = to_grid((double)z[j], (double)a.nf[2]);
+  g[0] = fold_grid((double)x[j] * a.gscale[0], (double)a.nf[0], a.ginv[0]);
+  g[1] = fold_grid((double)y[j] * a.gscale[1], (double)a.nf[1], a.ginv[1]);
+  if (a.dim == 3) g[2] = fold_grid((double)z[j] * a.gscale[2], (double)a.nf[2], a.ginv[2]);
   typename Cplx<T>::type zero;
   zero.x = 0;
   zero.y = 0;
-  emit_point<T>(a, g, 0, 0, scatter != 0, cursor, starts, recs, nullptr, zero, idx_out, (int)j,
-                cap, err);
+  emit_records<T>(a, g, 0, 0, scatter != 0, cursor, starts, recs, nullptr, zero, idx_out, (int)j,
+                  cap, err);
 }
 
 // Exclusive scan of n counts into starts[0..n], one CTA of 1024 threads.
@@ -374,6 +306,103 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// FP32, 3D, 16^3 tiles, compile-time kernel width W: the W kernel values per dimension stay in
+// registers and the support loops unroll completely, so a cell update is one multiply and
+// one shared-memory atomic; cells outside the tile are skipped by predicates.
+template <int W>
+__global__ void __launch_bounds__(256)
+    spread3_f32_w_kernel(SpreadArgs a, const RecF* __restrict__ recs, const int* __restrict__ idx,
+                         const float2* __restrict__ cv, int64_t c_stride,
+                         const int* __restrict__ starts, int real_pair,
+                         float2* __restrict__ fine) {
+  constexpr int TL = 16, CELLS = TL * TL * TL, NT = 256;
+  __shared__ __align__(16) float acc_re[CELLS];
+  __shared__ __align__(16) float acc_im[CELLS];
+  const int tid = threadIdx.x;
+  const int64_t key = blockIdx.x;
+  const int trans = blockIdx.y;
+  const int keygrid = (int)(key / a.n_tiles);
+  const int tile = (int)(key - (int64_t)keygrid * a.n_tiles);
+  const int tx = tile % a.ntile[0];
+  const int ty = (tile / a.ntile[0]) % a.ntile[1];
+  const int tz = tile / (a.ntile[0] * a.ntile[1]);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int c = tid; c < CELLS / 4; c += NT) {
+    reinterpret_cast<float4*>(acc_re)[c] = z4;
+    reinterpret_cast<float4*>(acc_im)[c] = z4;
+  }
+  __syncthreads();
+  const float beta = (float)a.beta;
+  const float s2w = 2.0f / (float)W;
+  const int r0 = starts[key], r1 = starts[key + 1];
+  for (int r = r0 + tid; r < r1; r += NT) {
+    const RecF rec = recs[r];
+    const float2 c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+    const int lx = (rec.packed & 0xff) - 64;
+    const int ly = ((rec.packed >> 8) & 0xff) - 64;
+    const int lz = ((rec.packed >> 16) & 0xff) - 64;
+    const int comp = (rec.packed >> 24) & 1;
+    float kx[W], ky[W], kz[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      kx[i] = es_eval<float>((rec.dx + (float)i) * s2w, beta);
+      ky[i] = es_eval<float>((rec.dy + (float)i) * s2w, beta);
+      kz[i] = es_eval<float>((rec.dz + (float)i) * s2w, beta);
+    }
+    if (real_pair) {
+      float* dst = comp ? acc_im : acc_re;
+#pragma unroll
+      for (int iz = 0; iz < W; ++iz) {
+        const int z = lz + iz;
+        if ((unsigned)z >= (unsigned)TL) continue;
+        const float vz = kz[iz] * c.x;
+#pragma unroll
+        for (int iy = 0; iy < W; ++iy) {
+          const int y = ly + iy;
+          if ((unsigned)y >= (unsigned)TL) continue;
+          const float vzy = vz * ky[iy];
+          const int row = (z * TL + y) * TL + lx;
+#pragma unroll
+          for (int ix = 0; ix < W; ++ix)
+            if ((unsigned)(lx + ix) < (unsigned)TL) atomicAdd(&dst[row + ix], vzy * kx[ix]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int iz = 0; iz < W; ++iz) {
+        const int z = lz + iz;
+        if ((unsigned)z >= (unsigned)TL) continue;
+#pragma unroll
+        for (int iy = 0; iy < W; ++iy) {
+          const int y = ly + iy;
+          if ((unsigned)y >= (unsigned)TL) continue;
+          const float vzy = kz[iz] * ky[iy];
+          const float sr = vzy * c.x, si = vzy * c.y;
+          const int row = (z * TL + y) * TL + lx;
+#pragma unroll
+          for (int ix = 0; ix < W; ++ix) {
+            if ((unsigned)(lx + ix) < (unsigned)TL) {
+              atomicAdd(&acc_re[row + ix], sr * kx[ix]);
+              atomicAdd(&acc_im[row + ix], si * kx[ix]);
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // two cells per 16-byte store
+  float4* out = reinterpret_cast<float4*>(fine + (int64_t)(keygrid + trans) * a.n_fine);
+  const int64_t nf0 = a.nf[0], nf1 = a.nf[1];
+  const int64_t x0 = (int64_t)tx * TL, y0 = (int64_t)ty * TL, z0 = (int64_t)tz * TL;
+  for (int c2 = tid; c2 < CELLS / 2; c2 += NT) {
+    const int c = 2 * c2;
+    const int x = c & (TL - 1), y = (c >> 4) & (TL - 1), z = c >> 8;
+    const float4 v = make_float4(acc_re[c], acc_im[c], acc_re[c + 1], acc_im[c + 1]);
+    out[(((z0 + z) * nf1 + (y0 + y)) * nf0 + (x0 + x)) >> 1] = v;
+  }
+}
+
 // Plan API deconvolution: fk[t][mode] = fine[t][k mod nf] / phihat(k), FINUFFT mode order.
 template <typename T>
 __global__ void deconv_plan_kernel(SpreadArgs a, int64_t m0, int64_t m1, int64_t m2,
@@ -461,6 +490,22 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
                               const int* idx, const typename Cplx<T>::type* cv, int64_t c_stride,
                               const int* starts, int nkeys, int ntrans, bool real_pair,
                               typename Cplx<T>::type* fine, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value && DIM == 3) {
+    if (a.tile[0] == 16 && a.tile[1] == 16 && a.tile[2] == 16 && a.w >= 3 && a.w <= 8) {
+      dim3 grid((unsigned)nkeys, (unsigned)ntrans);
+      const int rp = real_pair ? 1 : 0;
+      switch (a.w) {
+        case 3: spread3_f32_w_kernel<3><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+        case 4: spread3_f32_w_kernel<4><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+        case 5: spread3_f32_w_kernel<5><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+        case 6: spread3_f32_w_kernel<6><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+        case 7: spread3_f32_w_kernel<7><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+        default: spread3_f32_w_kernel<8><<<grid, 256, 0, s>>>(a, recs, idx, cv, c_stride, starts, rp, fine); break;
+      }
+      MPSQ_LAUNCH_CHECK();
+      return MPSQ_OK;
+    }
+  }
   size_t smem = spread_smem<T>(a, NT);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -608,6 +653,7 @@ extern "C" int mpsq_nufft_makeplan(int dim, const int64_t* n_modes, int iflag, i
   a.n_tiles = p->g.n_tiles;
   a.n_fine = p->g.n_fine;
   a.ngrid = 1;
+  finish_spread_args(a);
   const size_t csz = precision == MPSQ_FP64 ? sizeof(double2) : sizeof(float2);
   const size_t rsz = precision == MPSQ_FP64 ? sizeof(RecD) : sizeof(RecF);
   (void)rsz;
@@ -850,6 +896,7 @@ extern "C" int mpsq_nufft2d1_noalloc(int64_t nj, const double* x, const double* 
   a.n_tiles = (int64_t)a.ntile[0] * a.ntile[1];
   a.n_fine = nf0 * nf1;
   a.ngrid = 1;
+  finish_spread_args(a);
   const int64_t cap = 4 * std::max<int64_t>(nj, 1);
   // carve the scratch array
   unsigned char* q = base;
