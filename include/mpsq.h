@@ -155,6 +155,9 @@ typedef struct mpsq_job_desc {
   int32_t store_species;     /* 1: also keep per-species amplitudes (atom-pair mode)     */
   int32_t no_pack;           /* 0: when all strengths are real (q_center = 0) two species
                                 share one complex fine grid (re/im); 1: never pack        */
+  int32_t no_pruned_fft;     /* 0: FP32 volumes use the pruned three-pass fine-grid
+                                transform fused with the deconvolution; 1: cuFFT + separate
+                                deconvolution                                             */
 } mpsq_job_desc;
 
 typedef struct mpsq_job mpsq_job;

@@ -66,6 +66,7 @@ class JobDesc(C.Structure):
         ("n_frames", C.c_int32),
         ("store_species", C.c_int32),
         ("no_pack", C.c_int32),
+        ("no_pruned_fft", C.c_int32),
     ]
 
 

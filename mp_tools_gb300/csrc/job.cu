@@ -12,6 +12,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fft_smem.cuh"
 #include "mpsq_internal.h"
 
 namespace mpsq {
@@ -127,6 +128,11 @@ struct mpsq_job {
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   double stage_ms[4] = {0, 0, 0, 0};
   int64_t stage_frames = 0;
+  // pruned fine-grid transform (FP32, 3D)
+  bool pruned = false;
+  float2* tw[3] = {nullptr, nullptr, nullptr};
+  float2* b1 = nullptr;
+  int h[3] = {0, 0, 0}, K[3] = {1, 1, 1};
 };
 
 namespace mpsq {
@@ -348,6 +354,236 @@ __global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
   cs_frame[q] = out;
 }
 
+// ------------------------------------------------------------- pruned fine-grid transform
+// Only the 2h+1 central frequencies f in [-h, h] (h = m/2) of each dimension are needed
+// (modes -m/2..(m-1)/2 plus the mirror +m/2 that packed-pair separation reads), so the 3D
+// FFT runs as three passes that each keep 2h+1 of n outputs:
+//   X: fine (n2, n1, n0)   -> b1 (n2, n1, K0)
+//   Y: b1                  -> b2 (n2, K1, K0)
+//   Z: b2 column tiles and their mirror tiles -> deconvolution, pair separation, species
+//      weights, cs(t, Q)
+// K = 2h+1; frequency f is stored at index f + h.
+
+// Pass X: R contiguous rows of length N per CTA, one grid per blockIdx.y.
+template <int N, int R>
+__global__ void __launch_bounds__(256)
+    fftx_prune_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
+                      const float2* __restrict__ tw, int h0, int K0, float2* __restrict__ b1) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s0 = reinterpret_cast<float2*>(smem_raw);
+  float2* s1 = s0 + R * N;
+  const int g = blockIdx.y;
+  const int row0 = blockIdx.x * R;
+  const float4* src = reinterpret_cast<const float4*>(fine + (int64_t)g * n_fine + (int64_t)row0 * N);
+  const int rows = min(R, n_rows - row0);
+  for (int e = threadIdx.x; e < R * N / 2; e += blockDim.x) {  // two complex per load
+    const int line = e / (N / 2);
+    const float4 v = line < rows ? src[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+    s0[2 * e] = make_float2(v.x, v.y);
+    s0[2 * e + 1] = make_float2(v.z, v.w);
+  }
+  __syncthreads();
+  const float2* res = smem_fft<N, R, N, 1, false>(s0, s1, tw);
+  float2* dst = b1 + ((int64_t)g * n_rows + row0) * K0;
+  for (int e = threadIdx.x; e < rows * K0; e += blockDim.x) {
+    const int line = e / K0, i = e - line * K0;
+    const int f = i - h0;
+    dst[e] = res[line * N + (f < 0 ? f + N : f)];
+  }
+}
+
+// Pass Y: a tile of T consecutive x-columns (length N along y) of one z-plane per CTA.
+template <int N, int T>
+__global__ void __launch_bounds__(256)
+    ffty_prune_kernel(const float2* __restrict__ b1, int n2, int K0,
+                      const float2* __restrict__ tw, int h1, int K1, float2* __restrict__ b2) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s0 = reinterpret_cast<float2*>(smem_raw);
+  float2* s1 = s0 + T * N;
+  const int x0 = blockIdx.x * T, z = blockIdx.y, g = blockIdx.z;
+  const float2* src = b1 + ((int64_t)g * n2 + z) * N * K0;
+  for (int e = threadIdx.x; e < N * T; e += blockDim.x) {
+    const int y = e / T, c = e - y * T;
+    const int x = x0 + c;
+    s0[e] = x < K0 ? src[(int64_t)y * K0 + x] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const float2* res = smem_fft<N, T, 1, T, true>(s0, s1, tw);
+  float2* dst = b2 + ((int64_t)g * n2 + z) * K1 * K0;
+  for (int e = threadIdx.x; e < K1 * T; e += blockDim.x) {
+    const int i = e / T, c = e - i * T;
+    const int x = x0 + c;
+    if (x >= K0) continue;
+    const int f = i - h1;
+    dst[(int64_t)i * K0 + x] = res[(f < 0 ? f + N : f) * T + c];
+  }
+}
+
+// Pass Z fused with the deconvolution: CTA (x-tile, ky index iy) loads, for every grid, the T
+// z-columns (iy, x0..x0+T) and their mirrors (2h1-iy, 2h0-x), transforms all 2T lines, and
+// accumulates the weighted species amplitudes of the T x m2 output modes.
+template <int N, int T>
+__global__ void __launch_bounds__(256)
+    fftz_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
+                       int h0, int h1, int h2, int ngroups, const float2* __restrict__ tw,
+                       const float* __restrict__ c0, const float* __restrict__ c1,
+                       const float* __restrict__ c2, WeightArgs w, float2* __restrict__ cs_frame,
+                       float2* __restrict__ cs_species_frame) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NL = 2 * T;
+  float2* s0 = reinterpret_cast<float2*>(smem_raw);
+  float2* s1 = s0 + NL * N;
+  float2* acc = s1 + NL * N;  // [m2][T]
+  const int x0 = blockIdx.x * T, iy = blockIdx.y;
+  const int iym = 2 * h1 - iy;
+  const int64_t nm = (int64_t)m0 * m1 * m2;
+  for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
+  const float cy = c1[iy];
+  const int ky = iy - h1;
+  for (int g = 0; g < ngroups; ++g) {
+    const float2* src = b2 + (int64_t)g * N * K1 * K0;
+    const int pair = w.pair[g];
+    for (int e = threadIdx.x; e < N * NL; e += blockDim.x) {
+      const int z = e / NL, l = e - z * NL;
+      const int c = l < T ? l : l - T;
+      const int x = x0 + c;
+      float2 v = make_float2(0.f, 0.f);
+      if (x < m0 && (l < T || pair)) {
+        const int xi = l < T ? x : 2 * h0 - x;
+        const int yi = l < T ? iy : iym;
+        v = src[((int64_t)z * K1 + yi) * K0 + xi];
+      }
+      s0[e] = v;
+    }
+    __syncthreads();
+    const float2* res = smem_fft<N, NL, 1, NL, true>(s0, s1, tw);
+    const int sa = w.sp_a[g], sb = w.sp_b[g];
+    for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) {
+      const int iz = e / T, c = e - iz * T;
+      const int x = x0 + c;
+      if (x >= m0) continue;
+      const int fz = iz - h2;
+      const float2 G = res[(fz < 0 ? fz + N : fz) * NL + c];
+      const float corr = c0[x] * cy * c2[iz];
+      const int kx = x - h0, kz = fz;
+      float s2 = 0.f;
+      if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+        float qv[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+          qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
+        s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
+      }
+      float2 a = acc[e];
+      const int64_t q = ((int64_t)iz * m1 + iy) * m0 + x;
+      if (pair) {
+        const int mz = -fz;
+        const float2 Gm = res[(mz < 0 ? mz + N : mz) * NL + T + c];
+        const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
+        const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
+        const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
+        a.x += wa * ar + wb * br;
+        a.y += wa * ai + wb * bi;
+        if (w.store_species) {
+          cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
+          cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
+        }
+      } else {
+        const float wa = species_weight<float>(w, sa, s2);
+        a.x += wa * G.x * corr;
+        a.y += wa * G.y * corr;
+        if (w.store_species)
+          cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
+      }
+      acc[e] = a;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) {
+    const int iz = e / T, c = e - iz * T;
+    const int x = x0 + c;
+    if (x >= m0) continue;
+    const float2 a = acc[e];
+    cs_frame[((int64_t)iz * m1 + iy) * m0 + x] = make_float2(a.x * w.wnorm_f, a.y * w.wnorm_f);
+  }
+}
+
+// Tile sizes per transform length (shared memory: X 16*R*N, Y 16*T*N, Z 32*T*N + 8*T*m2 bytes)
+constexpr int prune_rx(int n) { return n <= 512 ? 8 : 4; }
+constexpr int prune_ty(int n) { return n <= 512 ? 8 : 4; }
+constexpr int prune_tz(int n) { return n <= 512 ? 4 : 2; }
+
+struct PruneLaunch {
+  const float2* fine;
+  int64_t n_fine;
+  float2* b1;
+  float2* b2;
+  int n[3], m[3], h[3], K[3];
+  int ngrid, ngroups;
+  const float2* tw[3];
+  const float* c[3];
+  cudaStream_t s;
+};
+
+template <int N>
+static int launch_prune_x(const PruneLaunch& p) {
+  constexpr int R = prune_rx(N);
+  const int n_rows = p.n[1] * p.n[2];
+  const size_t sm = (size_t)16 * R * N;
+  cudaFuncSetAttribute(fftx_prune_kernel<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  fftx_prune_kernel<N, R><<<dim3((unsigned)((n_rows + R - 1) / R), (unsigned)p.ngrid), 256, sm, p.s>>>(
+      p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
+  MPSQ_LAUNCH_CHECK();
+  return MPSQ_OK;
+}
+template <int N>
+static int launch_prune_y(const PruneLaunch& p) {
+  constexpr int T = prune_ty(N);
+  const size_t sm = (size_t)16 * T * N;
+  cudaFuncSetAttribute(ffty_prune_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  ffty_prune_kernel<N, T><<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)p.n[2], (unsigned)p.ngrid),
+                            256, sm, p.s>>>(p.b1, p.n[2], p.K[0], p.tw[1], p.h[1], p.K[1], p.b2);
+  MPSQ_LAUNCH_CHECK();
+  return MPSQ_OK;
+}
+template <int N>
+static int launch_prune_z(const PruneLaunch& p, const WeightArgs& w, float2* csf, float2* css) {
+  constexpr int T = prune_tz(N);
+  const size_t sm = (size_t)32 * T * N + (size_t)8 * T * p.m[2];
+  cudaFuncSetAttribute(fftz_deconv_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  fftz_deconv_kernel<N, T><<<dim3((unsigned)((p.m[0] + T - 1) / T), (unsigned)p.m[1]), 256, sm, p.s>>>(
+      p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.h[0], p.h[1], p.h[2], p.ngroups, p.tw[2],
+      p.c[0], p.c[1], p.c[2], w, csf, css);
+  MPSQ_LAUNCH_CHECK();
+  return MPSQ_OK;
+}
+
+static int run_pruned(const PruneLaunch& p, const WeightArgs& w, float2* csf, float2* css,
+                      cudaEvent_t mid) {
+  int rc = MPSQ_ERR_ARG;
+  switch (p.n[0]) {
+#define MPSQ_CASE(N) case N: rc = launch_prune_x<N>(p); break;
+    MPSQ_FFT_SIZES(MPSQ_CASE)
+#undef MPSQ_CASE
+  }
+  if (rc) return rc;
+  rc = MPSQ_ERR_ARG;
+  switch (p.n[1]) {
+#define MPSQ_CASE(N) case N: rc = launch_prune_y<N>(p); break;
+    MPSQ_FFT_SIZES(MPSQ_CASE)
+#undef MPSQ_CASE
+  }
+  if (rc) return rc;
+  if (mid) MPSQ_CUDA_TRY(cudaEventRecord(mid, p.s));
+  rc = MPSQ_ERR_ARG;
+  switch (p.n[2]) {
+#define MPSQ_CASE(N) case N: rc = launch_prune_z<N>(p, w, csf, css); break;
+    MPSQ_FFT_SIZES(MPSQ_CASE)
+#undef MPSQ_CASE
+  }
+  return rc;
+}
+
 static size_t csize(int prec) { return prec == MPSQ_FP64 ? sizeof(double2) : sizeof(float2); }
 static size_t rsize(int prec) { return prec == MPSQ_FP64 ? sizeof(RecD) : sizeof(RecF); }
 
@@ -414,6 +650,8 @@ static void job_free(mpsq_job* j) {
   cudaFree(j->cs);
   cudaFree(j->cs_species);
   cudaFree(j->err);
+  cudaFree(j->b1);
+  for (auto& t : j->tw) cudaFree(t);
   for (auto& e : j->ev)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -595,12 +833,40 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
     return fail(e == cudaErrorMemoryAllocation ? MPSQ_ERR_ALLOC : MPSQ_ERR_CUDA, "job_create: %s",
                 cudaGetErrorString(e));
   }
-  rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
-  if (rc) {
-    job_free(j);
-    return rc;
+  // Pruned fine-grid transform for FP32 volumes whose fine sizes factor into 2, 3, 5.
+  bool pruned = prec == MPSQ_FP32 && d->ndim == 3 && !d->no_pruned_fft;
+  for (int k = 0; k < 3 && pruned; ++k) pruned = fft_size_compiled((int)j->g.nf[k]);
+  if (pruned) {
+    for (int k = 0; k < 3; ++k) {
+      j->h[k] = (int)(j->g.m[k] / 2);
+      j->K[k] = 2 * j->h[k] + 1;
+    }
+    const int64_t n0 = j->g.nf[0], n1 = j->g.nf[1], n2 = j->g.nf[2];
+    e = cudaMalloc(&j->b1, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      std::vector<float2> t(j->g.nf[k]);
+      for (int64_t i = 0; i < j->g.nf[k]; ++i) {
+        const double ang = -2.0 * M_PI * (double)i / (double)j->g.nf[k];
+        t[i] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+      }
+      e = cudaMalloc(&j->tw[k], sizeof(float2) * t.size());
+      if (e == cudaSuccess)
+        e = cudaMemcpy(j->tw[k], t.data(), sizeof(float2) * t.size(), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+      job_free(j);
+      return fail(e == cudaErrorMemoryAllocation ? MPSQ_ERR_ALLOC : MPSQ_ERR_CUDA,
+                  "job_create (pruned transform): %s", cudaGetErrorString(e));
+    }
+    j->pruned = true;
+  } else {
+    rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
+    if (rc) {
+      job_free(j);
+      return rc;
+    }
+    j->have_fft = true;
   }
-  j->have_fft = true;
   *out = j;
   return MPSQ_OK;
 }
@@ -668,16 +934,42 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
                           (C*)j->fine, s);
     if (rc) return rc;
     if (mark(2)) return MPSQ_ERR_CUDA;
-    rc = exec_fft(j->fft, j->d.precision, j->fine, CUFFT_FORWARD);
-    if (rc) return rc;
-    if (mark(3)) return MPSQ_ERR_CUDA;
     C* csf = (C*)j->cs + (size_t)t * nm;
     C* css = j->cs_species ? (C*)j->cs_species + (size_t)t * j->d.n_species * nm : nullptr;
-    const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1], (unsigned)j->g.m[2]);
-    job_deconv_kernel<T><<<dgrid, 128, 0, s>>>(
-        a, (int)j->g.m[0], (int)j->g.m[1], (int)j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
-        (const T*)j->corr[1], (const T*)j->corr[2], j->wa, csf, css);
-    MPSQ_LAUNCH_CHECK();
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (j->pruned) {
+        PruneLaunch pl;
+        pl.fine = (const float2*)j->fine;
+        pl.n_fine = a.n_fine;
+        pl.b1 = j->b1;
+        pl.b2 = (float2*)j->fine;  // the fine grids are dead after pass X
+        for (int k = 0; k < 3; ++k) {
+          pl.n[k] = (int)j->g.nf[k];
+          pl.m[k] = (int)j->g.m[k];
+          pl.h[k] = j->h[k];
+          pl.K[k] = j->K[k];
+          pl.tw[k] = j->tw[k];
+          pl.c[k] = (const float*)j->corr[k];
+        }
+        pl.ngrid = a.ngrid;
+        pl.ngroups = j->ngroups;
+        pl.s = s;
+        rc = run_pruned(pl, j->wa, (float2*)csf, (float2*)css, prof ? j->ev[3] : nullptr);
+        if (rc) return rc;
+        done = true;
+      }
+    }
+    if (!done) {
+      rc = exec_fft(j->fft, j->d.precision, j->fine, CUFFT_FORWARD);
+      if (rc) return rc;
+      if (mark(3)) return MPSQ_ERR_CUDA;
+      const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1], (unsigned)j->g.m[2]);
+      job_deconv_kernel<T><<<dgrid, 128, 0, s>>>(
+          a, (int)j->g.m[0], (int)j->g.m[1], (int)j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
+          (const T*)j->corr[1], (const T*)j->corr[2], j->wa, csf, css);
+      MPSQ_LAUNCH_CHECK();
+    }
     if (prof) {
       if (mark(4)) return MPSQ_ERR_CUDA;
       MPSQ_CUDA_TRY(cudaEventSynchronize(j->ev[4]));

@@ -54,7 +54,7 @@ EsKernel es_params(double eps, int precision);
 // 1/phihat(k) for k = -m/2 .. (m-1)/2 on a fine grid of nf cells (Gauss-Legendre quadrature
 // of the kernel's Fourier integral).
 void es_correction(const EsKernel& es, int64_t nf, int64_t m, double* out);
-// Smallest fine size >= max(2m, 2w, tile) that is a multiple of tile with factors 2,3,5,7.
+// Smallest fine size >= max(2m, 2w, tile) that is a multiple of tile with factors 2, 3, 5.
 int64_t fine_size(int64_t m, int w, int tile);
 
 // --------------------------------------------------------------------- spreading layout

@@ -100,8 +100,8 @@ void es_correction(const EsKernel& es, int64_t nf, int64_t m, double* out) {
   }
 }
 
-static bool smooth7(int64_t n) {
-  for (int p : {2, 3, 5, 7})
+static bool smooth235(int64_t n) {
+  for (int p : {2, 3, 5})
     while (n % p == 0) n /= p;
   return n == 1;
 }
@@ -109,7 +109,7 @@ static bool smooth7(int64_t n) {
 int64_t fine_size(int64_t m, int w, int tile) {
   int64_t n = std::max<int64_t>({2 * m, 2 * (int64_t)w, (int64_t)tile});
   n = ((n + tile - 1) / tile) * tile;
-  while (!smooth7(n)) n += tile;
+  while (!smooth235(n)) n += tile;
   return n;
 }
 
@@ -306,19 +306,28 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// FP32, 3D, 16^3 tiles, compile-time kernel width W: the W kernel values per dimension stay in
-// registers and the support loops unroll completely, so a cell update is one multiply and
-// one shared-memory atomic; cells outside the tile are skipped by predicates.
+// FP32, 3D, 16^3 tiles, compile-time kernel width W, no atomics: thread (x, y) of the CTA owns
+// the 16-cell z-column (x, y, 0..15) of the tile in registers.  Records are staged in shared
+// memory in chunks with their x and y kernel values and their z kernel row already shifted
+// into tile coordinates (zeros outside the support); every thread then walks the chunk, and a
+// thread inside a record's x-y footprint adds 16 FMAs v * kz_row[z].  Warps whose two y-rows
+// miss the footprint skip the record (warp-uniform branch).  The tile is written once with
+// coalesced stores.
 template <int W>
 __global__ void __launch_bounds__(256)
     spread3_f32_w_kernel(SpreadArgs a, const RecF* __restrict__ recs, const int* __restrict__ idx,
                          const float2* __restrict__ cv, int64_t c_stride,
                          const int* __restrict__ starts, int real_pair,
                          float2* __restrict__ fine) {
-  constexpr int TL = 16, CELLS = TL * TL * TL, NT = 256;
-  __shared__ __align__(16) float acc_re[CELLS];
-  __shared__ __align__(16) float acc_im[CELLS];
+  constexpr int TL = 16, NT = 256, CH = 256;
+  __shared__ __align__(16) float s_kx[CH][8];
+  __shared__ __align__(16) float s_ky[CH][8];
+  __shared__ __align__(16) float s_kz[CH][TL];
+  __shared__ __align__(16) int4 s_meta[CH];     // lx, ly, comp, -
+  __shared__ __align__(16) float2 s_str[CH];
   const int tid = threadIdx.x;
+  const int x = tid & (TL - 1), y = tid >> 4;
+  const int wy0 = (tid >> 5) * 2;  // the two y-rows of this warp: wy0, wy0 + 1
   const int64_t key = blockIdx.x;
   const int trans = blockIdx.y;
   const int keygrid = (int)(key / a.n_tiles);
@@ -326,81 +335,95 @@ __global__ void __launch_bounds__(256)
   const int tx = tile % a.ntile[0];
   const int ty = (tile / a.ntile[0]) % a.ntile[1];
   const int tz = tile / (a.ntile[0] * a.ntile[1]);
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int c = tid; c < CELLS / 4; c += NT) {
-    reinterpret_cast<float4*>(acc_re)[c] = z4;
-    reinterpret_cast<float4*>(acc_im)[c] = z4;
+  float acc_re[TL], acc_im[TL];
+#pragma unroll
+  for (int z = 0; z < TL; ++z) {
+    acc_re[z] = 0.0f;
+    acc_im[z] = 0.0f;
   }
-  __syncthreads();
   const float beta = (float)a.beta;
   const float s2w = 2.0f / (float)W;
   const int r0 = starts[key], r1 = starts[key + 1];
-  for (int r = r0 + tid; r < r1; r += NT) {
-    const RecF rec = recs[r];
-    const float2 c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
-    const int lx = (rec.packed & 0xff) - 64;
-    const int ly = ((rec.packed >> 8) & 0xff) - 64;
-    const int lz = ((rec.packed >> 16) & 0xff) - 64;
-    const int comp = (rec.packed >> 24) & 1;
-    float kx[W], ky[W], kz[W];
+  for (int c0 = r0; c0 < r1; c0 += CH) {
+    const int n = min(CH, r1 - c0);
+    if (tid < n) {  // stage one record per thread
+      const int r = c0 + tid;
+      const RecF rec = recs[r];
+      const float2 c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+      const int lx = (rec.packed & 0xff) - 64;
+      const int ly = ((rec.packed >> 8) & 0xff) - 64;
+      const int lz = ((rec.packed >> 16) & 0xff) - 64;
+      const int comp = (rec.packed >> 24) & 1;
+      float kz[W];
 #pragma unroll
-    for (int i = 0; i < W; ++i) {
-      kx[i] = es_eval<float>((rec.dx + (float)i) * s2w, beta);
-      ky[i] = es_eval<float>((rec.dy + (float)i) * s2w, beta);
-      kz[i] = es_eval<float>((rec.dz + (float)i) * s2w, beta);
-    }
-    if (real_pair) {
-      float* dst = comp ? acc_im : acc_re;
-#pragma unroll
-      for (int iz = 0; iz < W; ++iz) {
-        const int z = lz + iz;
-        if ((unsigned)z >= (unsigned)TL) continue;
-        const float vz = kz[iz] * c.x;
-#pragma unroll
-        for (int iy = 0; iy < W; ++iy) {
-          const int y = ly + iy;
-          if ((unsigned)y >= (unsigned)TL) continue;
-          const float vzy = vz * ky[iy];
-          const int row = (z * TL + y) * TL + lx;
-#pragma unroll
-          for (int ix = 0; ix < W; ++ix)
-            if ((unsigned)(lx + ix) < (unsigned)TL) atomicAdd(&dst[row + ix], vzy * kx[ix]);
-        }
+      for (int i = 0; i < W; ++i) {
+        s_kx[tid][i] = es_eval<float>((rec.dx + (float)i) * s2w, beta);
+        s_ky[tid][i] = es_eval<float>((rec.dy + (float)i) * s2w, beta);
+        kz[i] = es_eval<float>((rec.dz + (float)i) * s2w, beta);
       }
-    } else {
 #pragma unroll
-      for (int iz = 0; iz < W; ++iz) {
-        const int z = lz + iz;
-        if ((unsigned)z >= (unsigned)TL) continue;
+      for (int z = 0; z < TL; ++z) {
+        float v = 0.0f;
 #pragma unroll
-        for (int iy = 0; iy < W; ++iy) {
-          const int y = ly + iy;
-          if ((unsigned)y >= (unsigned)TL) continue;
-          const float vzy = kz[iz] * ky[iy];
-          const float sr = vzy * c.x, si = vzy * c.y;
-          const int row = (z * TL + y) * TL + lx;
+        for (int i = 0; i < W; ++i) v = (z - lz == i) ? kz[i] : v;
+        s_kz[tid][z] = v;
+      }
+      s_meta[tid] = make_int4(lx, ly, comp, 0);
+      s_str[tid] = c;
+    }
+    __syncthreads();
+    for (int i = 0; i < n; ++i) {
+      const int4 m = s_meta[i];
+      if (wy0 + 1 < m.y || wy0 >= m.y + W) continue;  // warp-uniform: footprint misses our rows
+      const int dx = x - m.x, dy = y - m.y;
+      const bool act = (unsigned)dx < (unsigned)W && (unsigned)dy < (unsigned)W;
+      const float v = act ? s_kx[i][act ? dx : 0] * s_ky[i][act ? dy : 0] : 0.0f;
+      const float2 c = s_str[i];
+      const float4* kzr = reinterpret_cast<const float4*>(s_kz[i]);
+      if (real_pair) {
+        const float vv = v * c.x;
+        if (m.z == 0) {
 #pragma unroll
-          for (int ix = 0; ix < W; ++ix) {
-            if ((unsigned)(lx + ix) < (unsigned)TL) {
-              atomicAdd(&acc_re[row + ix], sr * kx[ix]);
-              atomicAdd(&acc_im[row + ix], si * kx[ix]);
-            }
+          for (int q = 0; q < TL / 4; ++q) {
+            const float4 k4 = kzr[q];
+            acc_re[4 * q + 0] = fmaf(vv, k4.x, acc_re[4 * q + 0]);
+            acc_re[4 * q + 1] = fmaf(vv, k4.y, acc_re[4 * q + 1]);
+            acc_re[4 * q + 2] = fmaf(vv, k4.z, acc_re[4 * q + 2]);
+            acc_re[4 * q + 3] = fmaf(vv, k4.w, acc_re[4 * q + 3]);
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < TL / 4; ++q) {
+            const float4 k4 = kzr[q];
+            acc_im[4 * q + 0] = fmaf(vv, k4.x, acc_im[4 * q + 0]);
+            acc_im[4 * q + 1] = fmaf(vv, k4.y, acc_im[4 * q + 1]);
+            acc_im[4 * q + 2] = fmaf(vv, k4.z, acc_im[4 * q + 2]);
+            acc_im[4 * q + 3] = fmaf(vv, k4.w, acc_im[4 * q + 3]);
           }
         }
+      } else {
+        const float vr = v * c.x, vi = v * c.y;
+#pragma unroll
+        for (int q = 0; q < TL / 4; ++q) {
+          const float4 k4 = kzr[q];
+          acc_re[4 * q + 0] = fmaf(vr, k4.x, acc_re[4 * q + 0]);
+          acc_re[4 * q + 1] = fmaf(vr, k4.y, acc_re[4 * q + 1]);
+          acc_re[4 * q + 2] = fmaf(vr, k4.z, acc_re[4 * q + 2]);
+          acc_re[4 * q + 3] = fmaf(vr, k4.w, acc_re[4 * q + 3]);
+          acc_im[4 * q + 0] = fmaf(vi, k4.x, acc_im[4 * q + 0]);
+          acc_im[4 * q + 1] = fmaf(vi, k4.y, acc_im[4 * q + 1]);
+          acc_im[4 * q + 2] = fmaf(vi, k4.z, acc_im[4 * q + 2]);
+          acc_im[4 * q + 3] = fmaf(vi, k4.w, acc_im[4 * q + 3]);
+        }
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
-  // two cells per 16-byte store
-  float4* out = reinterpret_cast<float4*>(fine + (int64_t)(keygrid + trans) * a.n_fine);
+  float2* out = fine + (int64_t)(keygrid + trans) * a.n_fine;
   const int64_t nf0 = a.nf[0], nf1 = a.nf[1];
-  const int64_t x0 = (int64_t)tx * TL, y0 = (int64_t)ty * TL, z0 = (int64_t)tz * TL;
-  for (int c2 = tid; c2 < CELLS / 2; c2 += NT) {
-    const int c = 2 * c2;
-    const int x = c & (TL - 1), y = (c >> 4) & (TL - 1), z = c >> 8;
-    const float4 v = make_float4(acc_re[c], acc_im[c], acc_re[c + 1], acc_im[c + 1]);
-    out[(((z0 + z) * nf1 + (y0 + y)) * nf0 + (x0 + x)) >> 1] = v;
-  }
+  const int64_t base = ((int64_t)tz * TL * nf1 + (int64_t)ty * TL + y) * nf0 + (int64_t)tx * TL + x;
+#pragma unroll
+  for (int z = 0; z < TL; ++z) out[base + (int64_t)z * nf1 * nf0] = make_float2(acc_re[z], acc_im[z]);
 }
 
 // Plan API deconvolution: fk[t][mode] = fine[t][k mod nf] / phihat(k), FINUFFT mode order.

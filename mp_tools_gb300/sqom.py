@@ -194,6 +194,7 @@ class SqomJob:
                  eps: float = 1e-6, weight_mode: int = _lib.WEIGHT_UNIT, b_coh=None, xff=None,
                  ff_convention: int = _lib.FF_MP_SQOM, mask=None, window: bool = False,
                  phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
+                 no_pruned_fft: bool = False,
                  n_atoms_frame: int | None = None, use_range: bool = False, eps_x: float = 0.1,
                  stream: int | None = None):
         L = _lib.load()
@@ -248,6 +249,7 @@ class SqomJob:
         d.n_frames = int(n_frames)
         d.store_species = int(store_species)
         d.no_pack = int(no_pack)
+        d.no_pruned_fft = int(no_pruned_fft)
         self.desc = d
         self.n_frames = int(n_frames)
         self.n_atoms_frame = d.n_atoms_frame

@@ -160,3 +160,25 @@ def test_bulk_xray_with_box_selection(cuda, ffc, kappa, prec, eps, tol):
                   ff_convention=ffc, eps_x=0.1)
     ref = oracle_cs(frames, counts, grid, weight_mode=3, xff=[XFF_AL, XFF_U], kappa=kappa, tol=0.1)
     assert rel_l2(job.amplitudes(), ref) < tol
+
+
+def test_pruned_transform_matches_cufft_path(cuda):
+    """FP32 volumes use the pruned three-pass transform fused with the deconvolution; it must
+    agree with cuFFT + the separate deconvolution kernel (5 species: two packed pairs and a
+    single grid)."""
+    frames, _, counts = cell_system(seed=7)
+    grid = QGrid(_lib.CELL, (4, 4, 4), n_bz=2, a_par=(4.19,) * 3, ndim=3)
+    kw = dict(precision=_lib.FP32, eps=1e-6, weight_mode=2, b_coh=[0.507, 0.716, 0.5803, 0.5803, 0.5803])
+    a = run_job(grid, frames, counts, **kw)
+    d = run_job(grid, frames, counts, no_pruned_fft=True, **kw)
+    assert rel_l2(a.amplitudes(), d.amplitudes()) < 3e-6
+
+
+@pytest.mark.parametrize("n_q", [(31, 47, 29), (30, 45, 64)])
+def test_pruned_transform_odd_and_mixed_mode_counts(cuda, n_q):
+    frames, _, counts = cell_system(F=2, seed=8)
+    grid = QGrid(_lib.CELL, (4, 4, 4), n_bz=2, a_par=(4.19,) * 3, ndim=3)
+    grid.n_q = n_q
+    job = run_job(grid, frames, counts, precision=_lib.FP32, eps=1e-6)
+    ref = oracle_cs(frames, counts, grid)
+    assert rel_l2(job.amplitudes(), ref) < 3e-5
