@@ -208,6 +208,20 @@ int mpsq_job_sqw_dispersion(mpsq_job* job, int32_t n_int, const float* t_wind,
 int mpsq_job_sqw_gauss(mpsq_job* job, double fwhm_frames, int32_t n_freq,
                        const float* q2_norm, double scale, float* out, int host);
 
+/* Spherical |Q| histogram of species pair products, mp_sql's Gauss integration
+ * (code/src/mp_sql56.f90:1224-1254): for every frame and every mode k with
+ * |Q| <= q_range, bin = nint(|Q| / q_step),
+ * out[(a*n_species + b)*n_hist + bin] += Re(A_a(k) conj(A_b(k))) with A_s the per-species
+ * amplitudes (job created with store_species = 1, or the weighted amplitude when
+ * n_species = 1) times `amp_scale`.  |Q| is formed in FP32 exactly as the reference's
+ * q_norm (code/src/mp_sql56.f90:1041): v = k * d_q per axis, Q = a_cell_inv v (row-major
+ * 3x3, left-to-right sums), |Q| by the scaled sum of squares of Fortran NORM2, with no
+ * fused multiply-adds, so that modes on a bin edge land in the reference's bin.
+ * out: n_species^2 x n_hist doubles. */
+int mpsq_job_radial_hist(mpsq_job* job, const double* a_cell_inv, const double* d_q,
+                         double q_step, double q_range, int32_t n_hist, double amp_scale,
+                         double* out, int host);
+
 /* Synchronise the job's stream. */
 int mpsq_job_sync(mpsq_job* job);
 

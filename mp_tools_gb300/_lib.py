@@ -27,7 +27,8 @@ EXPORTS = [
     "mpsq_job_create", "mpsq_job_destroy", "mpsq_job_estimate_bytes", "mpsq_job_set_frames",
     "mpsq_job_set_cell_index", "mpsq_job_transform", "mpsq_job_amplitudes", "mpsq_job_sq_total",
     "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_gauss", "mpsq_job_sync",
-    "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_last_error", "mpsq_version", "mpsq_launch_count",
+    "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
+    "mpsq_version", "mpsq_launch_count",
     "mpsq_nufft2d1_noalloc",
 ]
 
@@ -116,6 +117,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_job_sync": (C.c_int, [vp]),
         "mpsq_job_profile": (C.c_int, [vp, C.c_int]),
         "mpsq_job_stage_ms": (C.c_int, [vp, vp, vp, C.c_int]),
+        "mpsq_job_radial_hist": (C.c_int, [vp, vp, vp, dbl, dbl, i32, dbl, vp, C.c_int]),
         "mpsq_last_error": (C.c_char_p, []),
         "mpsq_version": (C.c_char_p, []),
         "mpsq_launch_count": (i64, []),

@@ -29,8 +29,8 @@ def nvcc() -> str:
 
 
 def _inputs() -> list[Path]:
-    return [CSRC / s for s in SOURCES] + [CSRC / "mpsq_internal.h", ROOT / "include" / "mpsq.h",
-                                          Path(__file__)]
+    return ([CSRC / s for s in SOURCES] + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
+            + [ROOT / "include" / "mpsq.h", Path(__file__)])
 
 
 def up_to_date() -> bool:

@@ -1036,6 +1036,8 @@ JobView job_view(mpsq_job* j) {
   v.n_q = j->g.n_modes;
   v.n_frames = j->d.n_frames;
   v.n_species = j->d.n_species;
+  for (int k = 0; k < 3; ++k) v.m[k] = j->g.m[k];
+  v.store_species = j->d.store_species;
   return v;
 }
 }  // namespace mpsq

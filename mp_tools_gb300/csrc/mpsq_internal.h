@@ -301,6 +301,8 @@ struct JobView {
   int64_t n_q;
   int32_t n_frames;
   int32_t n_species;
+  int64_t m[3];        // modes per dimension
+  int store_species;
 };
 }  // namespace mpsq
 struct mpsq_job;

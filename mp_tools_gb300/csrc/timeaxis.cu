@@ -508,3 +508,136 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
   cudaFree(dq);
   return rc;
 }
+
+// ------------------------------------------------------------- spherical |Q| histogram
+namespace mpsq {
+// Fortran NORM2 of a 3-vector as the scaled sum of squares (the recurrence of BLAS snrm2):
+// scale tracks the largest |component|, ssq the sum of squares relative to it.  Every
+// operation is a separately rounded FP32 op (no contraction into fused multiply-adds).
+__device__ __forceinline__ float norm2_scaled(float x, float y, float z) {
+  float scale = 0.0f, ssq = 1.0f;
+  const float c[3] = {x, y, z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float a = fabsf(c[i]);
+    if (a != 0.0f) {
+      if (scale < a) {
+        const float r = __fdiv_rn(scale, a);
+        ssq = __fadd_rn(1.0f, __fmul_rn(ssq, __fmul_rn(r, r)));
+        scale = a;
+      } else {
+        const float r = __fdiv_rn(a, scale);
+        ssq = __fadd_rn(ssq, __fmul_rn(r, r));
+      }
+    }
+  }
+  return __fmul_rn(scale, __fsqrt_rn(ssq));
+}
+
+__device__ __forceinline__ float dot3_rn(float3 a, float v0, float v1, float v2) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a.x, v0), __fmul_rn(a.y, v1)), __fmul_rn(a.z, v2));
+}
+
+// Grid-stride over modes; a CTA accumulates its bins in shared memory (FP32 partial sums of a
+// few thousand products) and flushes them to the FP64 output with atomics.
+template <typename T>
+__global__ void radial_hist_kernel(const typename Cplx<T>::type* __restrict__ amps, int s_stride,
+                                   int S, int64_t nq, int nt, int m0, int m1, int m2, float3 r0,
+                                   float3 r1, float3 r2, float3 dq, float q_step, float q_range,
+                                   int n_hist, float scale2, int use_smem,
+                                   double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* h = reinterpret_cast<float*>(smem_raw);
+  const int nb = S * S * n_hist;
+  if (use_smem) {
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) h[e] = 0.0f;
+    __syncthreads();
+  }
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % m0), j = (int)((q / m0) % m1), l = (int)(q / ((int64_t)m0 * m1));
+    // v = k * d_q, Q = a_cell_inv v, |Q| = NORM2(Q), all in FP32 (mp_sql56.f90:1041)
+    const float v0 = __fmul_rn((float)(i - m0 / 2), dq.x);
+    const float v1 = __fmul_rn((float)(j - m1 / 2), dq.y);
+    const float v2 = __fmul_rn((float)(l - m2 / 2), dq.z);
+    const float qn = norm2_scaled(dot3_rn(r0, v0, v1, v2), dot3_rn(r1, v0, v1, v2),
+                                  dot3_rn(r2, v0, v1, v2));
+    if (!(qn <= q_range)) continue;
+    const int bin = (int)roundf(__fdiv_rn(qn, q_step));   // NINT: half away from zero
+    if (bin < 0 || bin >= n_hist) continue;
+    for (int t = 0; t < nt; ++t) {
+      for (int a = 0; a < S; ++a) {
+        const auto A = amps[((int64_t)t * s_stride + a) * nq + q];
+        for (int b = 0; b < S; ++b) {
+          const auto B = amps[((int64_t)t * s_stride + b) * nq + q];
+          const float v = (float)(A.x * B.x + A.y * B.y) * scale2;
+          const int e = (a * S + b) * n_hist + bin;
+          if (use_smem)
+            atomicAdd(&h[e], v);
+          else
+            atomicAdd(&out[e], (double)v);
+        }
+      }
+    }
+  }
+  if (use_smem) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb; e += blockDim.x)
+      if (h[e] != 0.0f) atomicAdd(&out[e], (double)h[e]);
+  }
+}
+}  // namespace mpsq
+
+extern "C" int mpsq_job_radial_hist(mpsq_job* j, const double* a_cell_inv, const double* d_q,
+                                    double q_step, double q_range, int32_t n_hist,
+                                    double amp_scale, double* out, int host) {
+  if (!j || !a_cell_inv || !d_q || !out) return fail(MPSQ_ERR_ARG, "radial_hist: null pointer");
+  JobView v = job_view(j);
+  if (n_hist < 1 || !(q_step > 0)) return fail(MPSQ_ERR_ARG, "radial_hist: bad bins");
+  const void* amps = v.cs;
+  int S = 1, s_stride = 1;
+  if (v.store_species) {
+    amps = v.cs_species;
+    S = v.n_species;
+    s_stride = v.n_species;
+  } else if (v.n_species != 1) {
+    return fail(MPSQ_ERR_STATE, "radial_hist: per-species amplitudes need store_species = 1");
+  }
+  const size_t nb = (size_t)S * S * n_hist;
+  double* dev = nullptr;
+  MPSQ_CUDA_TRY(cudaMalloc(&dev, nb * sizeof(double)));
+  MPSQ_CUDA_TRY(cudaMemsetAsync(dev, 0, nb * sizeof(double), v.s));
+  const size_t smem = nb * sizeof(float);
+  const int use_smem = smem <= 96 * 1024 ? 1 : 0;
+  const double* A = a_cell_inv;
+  const float3 r0 = make_float3((float)A[0], (float)A[1], (float)A[2]);
+  const float3 r1 = make_float3((float)A[3], (float)A[4], (float)A[5]);
+  const float3 r2 = make_float3((float)A[6], (float)A[7], (float)A[8]);
+  const float3 dq = make_float3((float)d_q[0], (float)d_q[1], (float)d_q[2]);
+  const float scale2 = (float)(amp_scale * amp_scale);
+  const unsigned blocks = (unsigned)std::min<int64_t>((v.n_q + 255) / 256, 152 * 8);
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(radial_hist_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    radial_hist_kernel<double><<<blocks, 256, use_smem ? smem : 0, v.s>>>(
+        (const double2*)amps, s_stride, S, v.n_q, v.n_frames, (int)v.m[0], (int)v.m[1], (int)v.m[2],
+        r0, r1, r2, dq, (float)q_step, (float)q_range, n_hist, scale2, use_smem, dev);
+  } else {
+    cudaFuncSetAttribute(radial_hist_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    radial_hist_kernel<float><<<blocks, 256, use_smem ? smem : 0, v.s>>>(
+        (const float2*)amps, s_stride, S, v.n_q, v.n_frames, (int)v.m[0], (int)v.m[1], (int)v.m[2],
+        r0, r1, r2, dq, (float)q_step, (float)q_range, n_hist, scale2, use_smem, dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    if (host) {
+      e = cudaMemcpyAsync(out, dev, nb * sizeof(double), cudaMemcpyDeviceToHost, v.s);
+    } else {
+      e = cudaMemcpyAsync(out, dev, nb * sizeof(double), cudaMemcpyDeviceToDevice, v.s);
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(v.s);
+  cudaFree(dev);
+  if (e != cudaSuccess) return fail(MPSQ_ERR_CUDA, "radial_hist: %s", cudaGetErrorString(e));
+  return MPSQ_OK;
+}

@@ -317,6 +317,21 @@ class SqomJob:
         check(_lib.load().mpsq_job_stage_ms(self._h, ms, C.byref(fr), int(reset)), "stage_ms")
         return list(ms), int(fr.value)
 
+    def radial_hist(self, a_cell_inv, d_q, q_step: float, q_range: float, n_hist: int,
+                    amp_scale: float = 1.0) -> np.ndarray:
+        """Sum over frames and modes of Re(A_a conj A_b) binned by nint(|Q|/q_step) with
+        Q = a_cell_inv (k * d_q) (mp_sql's Gauss integration); returns
+        (n_species, n_species, n_hist)."""
+        S = len(self.species_counts) if self.desc.store_species else 1
+        out = np.zeros(S * S * n_hist, np.float64)
+        a = np.ascontiguousarray(np.asarray(a_cell_inv, np.float64).reshape(9))
+        d = np.ascontiguousarray(np.asarray(d_q, np.float64).reshape(3))
+        check(_lib.load().mpsq_job_radial_hist(self._h, C.c_void_p(ptr(a)), C.c_void_p(ptr(d)),
+                                               float(q_step), float(q_range), int(n_hist),
+                                               float(amp_scale), C.c_void_p(ptr(out)), 1),
+              "radial_hist")
+        return out.reshape(S, S, n_hist)
+
     def amplitudes_ptr(self) -> int:
         p = C.c_void_p()
         check(_lib.load().mpsq_job_amplitudes(self._h, C.byref(p)), "amplitudes")

@@ -1,0 +1,141 @@
+"""Golden-file parity on the reference's amorphous Al92U8 example (mp_sql, X-ray weights).
+
+The fixtures under tests/golden/alu are the reference's own input frame
+(examples/amorphous_Al92U08/data/Al_U_large_n0001.dat: 30,000 atoms, cubic 79.816 A box) and
+the numbers of its four output tables Al_U_large_sql_0001_40..43.txt: Z(Q), I(Q), S(Q) and
+unscaled I(Q) with total and partial columns, Q = 0.55..20 A^-1 in 0.01 steps, Gaussian
+smoothing FWHM 0.05 A^-1.  They were produced by MP_TOOLS 1.56 (gfortran, FINUFFT at eps 1e-6)
+and are printed with 9 significant digits.
+
+* CPU: the oracle (FP64 ES NUFFT at eps 1e-9, FP32 |Q| binning, numpy restatement of the
+  normalisation/smoothing/weighting of code/src/mp_sql56.f90:1224-1521) reproduces every
+  column for Q <= 7.9 within 2e-6 of the column's largest value; the product's host-side
+  post-processing (mp_tools_gb300.sql.scattering_functions) equals the oracle's.
+* GPU: the product path (per-species 3D NUFFT job, device |Q| histogram, host
+  post-processing) reproduces every column over the whole Q range.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mp_tools_gb300 import io, synth
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "alu"
+TABLES = (("t40", 5), ("t41", 6), ("t42", 4), ("t43", 7))
+Q_RANGE_FULL = 20.0        # the last printed row of the reference tables
+Q_RANGE_CPU = 8.0          # oracle case: 205^3 modes, a few seconds on the host
+
+
+def _setup():
+    f = io.read_dat(GOLDEN / "Al_U_large_n0001.dat")
+    meta = json.loads((GOLDEN / "sql_golden.json").read_text())
+    g = np.load(GOLDEN / "sql_golden.npz")
+    par = io.read_par(GOLDEN / "Al_U_large.par")
+    q_step = next(grp["q_step"] for grp in par.values() if isinstance(grp, dict) and "q_step" in grp)
+    fwhm = int(round(meta["43"]["smooth_fwhm_A"] / q_step))
+    counts = f.species_counts()
+    box = float(np.float32(f.header["a_par"][0]))
+    return dict(frame=f, tables=g, q_step=float(q_step), fwhm=fwhm, counts=counts, box=box,
+                n_tot=f.n_tot, occ=np.asarray(counts, float) / f.n_tot,
+                xff=[synth.XFF["Al"], synth.XFF["U"]])
+
+
+def _columns(total, parts):
+    cols = [] if total is None else [total]
+    return cols + [parts[k] for k in sorted(parts)]     # (0,0), (1,0), (1,1) as printed
+
+
+def _compare(setup, hist, q_max, post, tol):
+    """Worst |computed - golden| / max|golden| per column of every table, rows Q <= q_max."""
+    worst = 0.0
+    for key, mode in TABLES:
+        G = setup["tables"][key]
+        q, total, parts = post(hist, mode)
+        rows = int(np.sum(G[:, 0] <= q_max + 1e-6))
+        assert np.allclose(q[:rows], G[:rows, 0], atol=1e-6), key
+        cols = _columns(total, parts)
+        assert len(cols) == G.shape[1] - 1, key
+        for c, col in enumerate(cols):
+            ref = G[:rows, c + 1]
+            err = np.max(np.abs(col[:rows] - ref)) / np.max(np.abs(ref))
+            worst = max(worst, err)
+            assert err <= tol, f"{key} column {c + 1}: {err:.2e} > {tol:.1e}"
+    return worst
+
+
+def _oracle_post(setup):
+    from oracle import sql_ref
+
+    def post(hist, mode):
+        return sql_ref.xray_total_and_partials(
+            hist, q_step=setup["q_step"], nfile=1, at_volume=setup["box"] ** 3 / setup["n_tot"],
+            occ=setup["occ"], xff=setup["xff"], mode=mode, fwhm=setup["fwhm"])
+    return post
+
+
+def _product_post(setup):
+    from mp_tools_gb300 import sql
+
+    def post(hist, mode):
+        return sql.scattering_functions(
+            hist, q_step=setup["q_step"], nfile=1, at_volume=setup["box"] ** 3 / setup["n_tot"],
+            occ=setup["occ"], mode=mode, weight="xray", xff=setup["xff"],
+            n_smooth_fwhm=setup["fwhm"])
+    return post
+
+
+@pytest.fixture(scope="module")
+def oracle_hist():
+    from oracle import sql_ref
+    s = _setup()
+    n, d_q = sql_ref.cube(Q_RANGE_CPU, s["box"])
+    off = np.concatenate([[0], np.cumsum(s["counts"])])
+    amps = [sql_ref.amplitudes(s["frame"].at_pos, off[a], off[a + 1], n, d_q, eps=1e-9) / s["n_tot"]
+            for a in range(len(s["counts"]))]
+    return s, sql_ref.histogram(amps, n, d_q, s["q_step"], Q_RANGE_CPU)
+
+
+def test_oracle_pinned_by_reference_tables(oracle_hist):
+    s, hist = oracle_hist
+    worst = _compare(s, hist, Q_RANGE_CPU - 0.1, _oracle_post(s), tol=2e-6)
+    assert worst < 2e-6
+
+
+def test_host_postprocessing_equals_oracle(oracle_hist):
+    """mp_tools_gb300.sql.scattering_functions (product) vs the oracle restatement on the
+    same histogram: identical up to FP64 rounding, for all four output modes."""
+    s, hist = oracle_hist
+    for key, mode in TABLES:
+        q0, t0, p0 = _oracle_post(s)(hist, mode)
+        q1, t1, p1 = _product_post(s)(hist, mode)
+        assert np.array_equal(q0, q1)
+        for a, b in zip(_columns(t0, p0), _columns(t1, p1)):
+            np.testing.assert_allclose(b, a, rtol=1e-12, atol=1e-12 * np.max(np.abs(a)))
+
+
+def test_grid_matches_reference_cube():
+    """mp_sql's Q cube (code/src/mp_sql56.f90:975-1019) for the golden run: 509^3 modes."""
+    from mp_tools_gb300 import sql
+    from oracle import sql_ref
+    s = _setup()
+    grid = sql.SqlGrid(Q_RANGE_FULL, (s["box"],) * 3)
+    n, d_q = sql_ref.cube(Q_RANGE_FULL, s["box"])
+    assert grid.n_q == (n, n, n) == (509, 509, 509)
+    assert np.allclose(grid.d_q, d_q, rtol=0, atol=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_gpu_job_reproduces_reference_tables(cuda, precision):
+    from mp_tools_gb300 import _lib, sql
+    s = _setup()
+    grid = sql.SqlGrid(Q_RANGE_FULL, (s["box"],) * 3)
+    frames = s["frame"].at_pos[None, :, :]
+    prec = _lib.FP32 if precision == "fp32" else _lib.FP64
+    hist = sql.transform_histogram(frames, s["counts"], grid, s["q_step"], precision=prec,
+                                   eps=1e-6 if precision == "fp32" else 1e-9)
+    # FP32 amplitudes at eps 1e-6 against tables printed from an eps 1e-6 FP64 run
+    tol = 2e-5 if precision == "fp32" else 5e-6
+    _compare(s, hist, Q_RANGE_FULL, _product_post(s), tol=tol)

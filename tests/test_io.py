@@ -1,0 +1,139 @@
+"""Frame-file, parameter-file and text-map formats (CPU).
+
+The .dat layout follows code/src/mp_latt56.f90:295-343 (4096-byte records, namelist header
+records, at_ind int32 x 4 then at_pos float32 x 4, 256 atoms per record); the map body
+follows code/src/mp_sqom56.f90:1995-2045 (format 200(1x,5e10.3)).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mp_tools_gb300 import io
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+ALU_DAT = GOLDEN / "alu" / "Al_U_large_n0001.dat"
+
+
+def test_read_reference_frame_file():
+    f = io.read_dat(ALU_DAT)
+    assert f.n_tot == 30000
+    assert f.species_counts() == [27600, 2400]
+    assert f.at_pos.dtype == np.float32 and f.at_pos.shape == (30000, 4)
+    assert f.at_ind.dtype == np.int32 and f.at_ind.shape == (30000, 4)
+    a_par = np.asarray(f.header["a_par"], np.float64)
+    assert np.allclose(a_par, 79.815962, rtol=1e-6)
+    # positions lie in the box centred on the origin, species-major: all Al (1) before U (2)
+    half = 0.5 * a_par[0] + 1e-3
+    assert f.at_pos[:, :3].min() >= -half and f.at_pos[:, :3].max() <= half
+    assert np.all(np.diff(f.at_ind[:, 3]) >= 0)
+    assert set(np.unique(f.at_ind[:, 3])) == {1, 2}
+
+
+def test_dat_round_trip_is_bit_exact(tmp_path):
+    f = io.read_dat(ALU_DAT)
+    out = tmp_path / "copy_n0001.dat"
+    io.write_dat(out, f)
+    g = io.read_dat(out)
+    assert out.stat().st_size % io.REC_BYTES == 0
+    assert g.n_tot == f.n_tot and g.species_counts() == f.species_counts()
+    assert np.array_equal(g.at_pos.view(np.uint32), f.at_pos.view(np.uint32))
+    assert np.array_equal(g.at_ind, f.at_ind)
+    for k in ("a_par", "n_tot", "nsuper_r", "input_method"):
+        if k in f.header:
+            assert g.header[k] == f.header[k], k
+
+
+def test_dat_ragged_last_record(tmp_path):
+    """n_tot not a multiple of 256: the last record is zero-padded and ignored on read."""
+    rng = np.random.default_rng(7)
+    n = 300
+    pos = rng.random((n, 4), dtype=np.float32)
+    ind = np.zeros((n, 4), np.int32)
+    ind[:, 3] = np.repeat([1, 2], [200, 100])
+    hdr = {"sim_type": "synthetic", "input_method": "BULK", "a_par": [1.0, 1.0, 1.0],
+           "n_atom": 2, "nsuper_r": [200, 100], "at_name_out": ["Al", "U"]}
+    f = io.DatFrame(header=hdr, at_ind=ind, at_pos=pos)
+    p = tmp_path / "r_n0001.dat"
+    io.write_dat(p, f)
+    assert p.stat().st_size == (4 + 2 * 2) * io.REC_BYTES
+    g = io.read_dat(p)
+    assert np.array_equal(g.at_pos, pos) and np.array_equal(g.at_ind, ind)
+
+
+def test_dat_rejects_corrupt_files(tmp_path):
+    data = ALU_DAT.read_bytes()
+    p = tmp_path / "bad.dat"
+    p.write_bytes(data[:-io.REC_BYTES])          # truncated position block
+    with pytest.raises(ValueError):
+        io.read_dat(p)
+    p.write_bytes(data[:1000])                   # not a whole record
+    with pytest.raises(ValueError):
+        io.read_dat(p)
+    p.write_bytes(b"XX" + data[2:])              # wrong magic
+    with pytest.raises(ValueError):
+        io.read_dat(p)
+
+
+def test_trajectory_naming_and_reading(tmp_path):
+    f = io.read_dat(ALU_DAT)
+    for i in (1, 2, 3):
+        g = io.DatFrame(header=dict(f.header, t_dump=0.01 * i), at_ind=f.at_ind,
+                        at_pos=f.at_pos + np.float32(i))
+        io.write_dat(io.frame_file(tmp_path, "traj", i), g)
+    assert io.frame_file(tmp_path, "traj", 12).name == "traj_n0012.dat"
+    frames, f0, t_step = io.read_trajectory(tmp_path, "traj", 1, 3)
+    assert frames.shape == (3, 30000, 4)
+    assert np.array_equal(frames[2], f.at_pos + np.float32(3))
+    assert t_step == pytest.approx(0.01)
+
+
+def test_read_par_namelist_and_atoms():
+    p = io.read_par(GOLDEN / "alu" / "Al_U_large.par")
+    flat = {}
+    for grp in p.values():
+        if isinstance(grp, dict):
+            flat.update(grp)
+    assert flat["j_weight"] == 3
+    assert flat["q_step"] == pytest.approx(0.01)
+    labels = [a[0] for a in p["atoms"]]
+    assert labels[:2] == ["Al", "U"]
+
+
+def test_namelist_parse_format_round_trip():
+    items = {"a_par": [79.815962, 79.815962, 79.815962], "n_tot": 30000,
+             "subst_name": "Al_U", "nsuper_r": [27600, 2400]}
+    text = io.format_namelist("data_header_1", items)
+    back = io.parse_namelist(text)["data_header_1"]
+    assert back["n_tot"] == 30000 and back["nsuper_r"] == [27600, 2400]
+    assert back["subst_name"] == "Al_U"
+    assert np.allclose(back["a_par"], items["a_par"])
+
+
+def test_fortran_e_edit_descriptor():
+    assert io.fortran_e(0.000242) == " 0.242E-03"
+    assert io.fortran_e(-1234.5) == "-0.123E+04"
+    assert io.fortran_e(0.0) == " 0.000E+00"
+    assert io.fortran_e(0.9996) == " 0.100E+01"      # rounding carries into a new digit
+    assert io.fortran_e(1.5e-120) == " 0.150-119"    # three-digit exponent drops the E
+    assert io.fortran_e(float("nan")) == "*" * 10
+
+
+def test_map_rows_match_reference_output():
+    """Three body lines of the reference's BZO map: parsed and re-emitted byte for byte."""
+    lines = (GOLDEN / "bzo_map_rows.txt").read_text().splitlines()
+    vals = np.array([[io._fix_exp(t) for t in ln.split()] for ln in lines])
+    assert vals.shape[1] == 160
+    assert io.format_map_rows(vals) == lines
+
+
+def test_sq_table_write_read(tmp_path):
+    rng = np.random.default_rng(3)
+    m = rng.random((12, 7)) * 10.0 ** rng.integers(-5, 5, (12, 7))
+    p = tmp_path / "map.txt"
+    io.write_sq_table(p, m, substance="test", atoms=("Al", "U"), b_coh=(0.345, 0.842),
+                      masks=(1, 1))
+    back = io.read_sq_table(p)
+    assert back.shape == m.shape
+    # a 0.ddd mantissa keeps 3 digits: relative rounding error <= 0.0005/0.100
+    assert np.allclose(back, m, rtol=5.01e-3, atol=0.0)
