@@ -118,6 +118,22 @@ def measured_peaks():
 
 
 # ----------------------------------------------------------------------------- workload
+SPREAD_KERNEL = "spread3_pair_mma_kernel<7>"
+SPREAD_PROFILE = ROOT / "profiles" / "spread3_pair_mma_w7_alu1e6_192.txt"
+
+
+def profiled_traffic():
+    """DRAM bytes (read + write) per launch of the spread kernel, from the committed summary
+    of an ncu capture of this workload (line 'traffic_bytes_per_launch: N')."""
+    try:
+        for line in SPREAD_PROFILE.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1]), SPREAD_PROFILE.name
+    except OSError:
+        pass
+    return None, None
+
+
 def make_workload(device="cuda"):
     from mp_tools_gb300 import synth
     t0 = time.time()
@@ -296,11 +312,13 @@ def run_gpu(args):
     launches0 = L.mpsq_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
+    torch.cuda.nvtx.range_push("bench_timed")   # lets a profiler select the timed launches
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     barrier()
+    torch.cuda.nvtx.range_pop()
     launches = L.mpsq_launch_count() - launches0
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
@@ -318,8 +336,9 @@ def run_gpu(args):
     host_sq = torch.empty(sq.shape, dtype=torch.float32, pin_memory=True)
 
     def step_e2e():
-        job.set_frames(host_frames)
-        step()
+        job.transform_from_host(host_frames)    # chunked upload overlapping the transform
+        job.sq_total(out=sq)
+        job.sqw_gauss(fwhm_frames=FRAMES / 2, n_freq=n_freq, t_step=T_STEP, out=sqw)
         host_sqw.copy_(sqw, non_blocking=True)
         host_sq.copy_(sq, non_blocking=True)
 
@@ -349,9 +368,10 @@ def run_gpu(args):
     n_fine = 384 ** 3
     spread_bytes = sum(counts) * 16 + n_fine * 8
     achieved = spread_bytes / (stage["spread"] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "spread_tile_kernel<float,3>", "achieved": achieved,
+    traffic, traffic_src = profiled_traffic()
+    roofline = {"bound": "hbm", "kernel": SPREAD_KERNEL, "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": None,
+                "traffic": traffic, "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": spread_bytes,
                 "ms_per_launch": stage["spread"],
                 "stages_ms_per_frame": stage}
@@ -434,7 +454,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mpsq", choices=["mpsq", "reference"])
-    ap.add_argument("--cpu-frames", type=int, default=1)
+    ap.add_argument("--cpu-frames", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")

@@ -174,6 +174,12 @@ int mpsq_job_estimate_bytes(const mpsq_job_desc* desc, int64_t* bytes);
  * host == 0: pos is a device pointer (copied D2D). */
 int mpsq_job_set_frames(mpsq_job* job, const float* pos, int32_t first, int32_t count,
                         int host);
+/* The same copy issued on `stream` (a cudaStream_t other than the job's, so that uploads of
+ * later frames overlap the transform of earlier ones).  The caller orders it against the job's
+ * stream, e.g. with an event recorded after the copy and waited on before mpsq_job_transform
+ * of those frames; host memory should be pinned for the copy to run asynchronously. */
+int mpsq_job_set_frames_on(mpsq_job* job, const float* pos, int32_t first, int32_t count,
+                           int host, void* stream);
 /* Optional cell indices at_ind (int32 x4 per atom, frame independent) for CELL selection. */
 int mpsq_job_set_cell_index(mpsq_job* job, const int32_t* at_ind, int host);
 

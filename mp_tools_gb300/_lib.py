@@ -25,6 +25,7 @@ EXPORTS = [
     "mpsq_nufft_makeplan", "mpsq_nufft_setpts", "mpsq_nufft_execute", "mpsq_nufft_destroy",
     "mpsq_nufft_info", "mpsq_nufft_check_error",
     "mpsq_job_create", "mpsq_job_destroy", "mpsq_job_estimate_bytes", "mpsq_job_set_frames",
+    "mpsq_job_set_frames_on",
     "mpsq_job_set_cell_index", "mpsq_job_transform", "mpsq_job_amplitudes", "mpsq_job_sq_total",
     "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_gauss", "mpsq_job_sync",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
@@ -107,6 +108,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_job_destroy": (C.c_int, [vp]),
         "mpsq_job_estimate_bytes": (C.c_int, [vp, vp]),
         "mpsq_job_set_frames": (C.c_int, [vp, vp, i32, i32, C.c_int]),
+        "mpsq_job_set_frames_on": (C.c_int, [vp, vp, i32, i32, C.c_int, vp]),
         "mpsq_job_set_cell_index": (C.c_int, [vp, vp, C.c_int]),
         "mpsq_job_transform": (C.c_int, [vp, i32, i32]),
         "mpsq_job_amplitudes": (C.c_int, [vp, vp]),

@@ -1,49 +1,12 @@
-// Shared-memory FFT building blocks for the pruned fine-grid transform: a self-sorting
-// (Stockham) forward DFT of `nl` lines of length n = 2^a 3^b 5^c held in shared memory, with
-// radix-4/2/3/5 stages and a precomputed twiddle table tw[k] = exp(-2 pi i k / n).
-//
-// Stage recurrence (DIT, L = product of the radices already applied, Ls = L r, m = n/Ls):
-//   out[k*Ls + j + q*L] = sum_p w_r^{qp} ( w_Ls^{jp} in[(k + m p)*L + j] ),
-//   j in [0, L), k in [0, m), q in [0, r); after the last stage out[f] = DFT[f].
+// Shared-memory FFT building blocks for the pruned fine-grid transform and the time-axis
+// spectrum: forward DFTs of lines of length n = 2^a 3^b 5^c held in shared memory, computed in
+// place by mixed-radix decimation in frequency (radix 8, 6, 4, 2, 3, 5 butterflies) with a
+// twiddle table tw[k] = exp(-2 pi i k / n); outputs are read at digit-reversed positions.
 #pragma once
 
 #include <cuda_runtime.h>
 
 namespace mpsq {
-
-constexpr int kMaxFftStages = 24;
-
-struct SmemFftPlan {
-  int n = 0;
-  int nst = 0;
-  int radix[kMaxFftStages] = {};
-};
-
-// Radices in application order; false if n has a prime factor other than 2, 3, 5.
-inline bool make_smem_fft_plan(int n, SmemFftPlan* p) {
-  SmemFftPlan q;
-  q.n = n;
-  int r = n;
-  while (r % 4 == 0 && q.nst < kMaxFftStages) {
-    q.radix[q.nst++] = 4;
-    r /= 4;
-  }
-  while (r % 2 == 0 && q.nst < kMaxFftStages) {
-    q.radix[q.nst++] = 2;
-    r /= 2;
-  }
-  while (r % 3 == 0 && q.nst < kMaxFftStages) {
-    q.radix[q.nst++] = 3;
-    r /= 3;
-  }
-  while (r % 5 == 0 && q.nst < kMaxFftStages) {
-    q.radix[q.nst++] = 5;
-    r /= 5;
-  }
-  if (r != 1) return false;
-  *p = q;
-  return true;
-}
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -96,51 +59,147 @@ __device__ __forceinline__ void butterfly(float2* v, int r) {
   }
 }
 
-// Compile-time Stockham stages: transform length N and line count NL are template
-// parameters so every index computation reduces to shifts and multiply-adds.  Element
-// (line, i) lives at buf[line*LS + i*ES].  LINE_FAST maps consecutive threads to consecutive
-// lines (lines adjacent in memory), otherwise to consecutive butterflies of one line.
-template <int N>
-constexpr int next_radix(int rem) {
-  return rem % 4 == 0 ? 4 : (rem % 2 == 0 ? 2 : (rem % 3 == 0 ? 3 : 5));
+// Forward 8-point DFT in place: v[k'] = sum_k v[k] exp(-2 pi i k k'/8), as two 4-point DFTs
+// of the even and odd samples combined with w8^k' = exp(-i pi k'/4).
+__device__ __forceinline__ void dft8(float2* v) {
+  const float r = 0.70710678118654752440f;
+  float2 e[4], o[4];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float2 a0 = v[h], a1 = v[h + 2], a2 = v[h + 4], a3 = v[h + 6];
+    const float2 b0 = make_float2(a0.x + a2.x, a0.y + a2.y);
+    const float2 b1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+    const float2 b2 = make_float2(a1.x + a3.x, a1.y + a3.y);
+    const float2 b3 = make_float2(a1.x - a3.x, a1.y - a3.y);
+    float2* d = h ? o : e;
+    d[0] = make_float2(b0.x + b2.x, b0.y + b2.y);
+    d[2] = make_float2(b0.x - b2.x, b0.y - b2.y);
+    d[1] = make_float2(b1.x + b3.y, b1.y - b3.x);   // b1 - i b3
+    d[3] = make_float2(b1.x - b3.y, b1.y + b3.x);   // b1 + i b3
+  }
+  const float2 t1 = make_float2((o[1].x + o[1].y) * r, (o[1].y - o[1].x) * r);    // w8 o1
+  const float2 t2 = make_float2(o[2].y, -o[2].x);                                 // -i o2
+  const float2 t3 = make_float2((o[3].y - o[3].x) * r, -(o[3].x + o[3].y) * r);   // w8^3 o3
+  v[0] = make_float2(e[0].x + o[0].x, e[0].y + o[0].y);
+  v[4] = make_float2(e[0].x - o[0].x, e[0].y - o[0].y);
+  v[1] = make_float2(e[1].x + t1.x, e[1].y + t1.y);
+  v[5] = make_float2(e[1].x - t1.x, e[1].y - t1.y);
+  v[2] = make_float2(e[2].x + t2.x, e[2].y + t2.y);
+  v[6] = make_float2(e[2].x - t2.x, e[2].y - t2.y);
+  v[3] = make_float2(e[3].x + t3.x, e[3].y + t3.y);
+  v[7] = make_float2(e[3].x - t3.x, e[3].y - t3.y);
 }
 
-template <int N, int L, int NL, int LS, int ES, bool LINE_FAST>
-struct StockhamStages {
-  static __device__ __forceinline__ float2* run(float2* in, float2* out,
-                                                const float2* __restrict__ tw) {
-    if constexpr (L >= N) {
-      return in;
-    } else {
-      constexpr int r = next_radix<N>(N / L);
-      constexpr int Ls = L * r, m = N / Ls, nb = N / r;
-      for (int e = threadIdx.x; e < nb * NL; e += blockDim.x) {
-        const int line = LINE_FAST ? e % NL : e / nb;
-        const int b = LINE_FAST ? e / NL : e % nb;
-        const int j = b % L, k = b / L;
-        float2 v[5];
-        const float2* src = in + line * LS;
+// Forward 6-point DFT in place: two 3-point DFTs of the even and odd samples combined with
+// w6^k' = exp(-i pi k'/3).
+__device__ __forceinline__ void dft6(float2* v) {
+  float2 e[3] = {v[0], v[2], v[4]}, o[3] = {v[1], v[3], v[5]};
+  butterfly(e, 3);
+  butterfly(o, 3);
+  const float h = 0.5f, s = 0.86602540378443864676f;
+  const float2 t1 = make_float2(h * o[1].x + s * o[1].y, h * o[1].y - s * o[1].x);    // w6 o1
+  const float2 t2 = make_float2(-h * o[2].x + s * o[2].y, -h * o[2].y - s * o[2].x);  // w6^2 o2
+  v[0] = make_float2(e[0].x + o[0].x, e[0].y + o[0].y);
+  v[3] = make_float2(e[0].x - o[0].x, e[0].y - o[0].y);
+  v[1] = make_float2(e[1].x + t1.x, e[1].y + t1.y);
+  v[4] = make_float2(e[1].x - t1.x, e[1].y - t1.y);
+  v[2] = make_float2(e[2].x + t2.x, e[2].y + t2.y);
+  v[5] = make_float2(e[2].x - t2.x, e[2].y - t2.y);
+}
+
+// Radices of an in-place decimation-in-frequency transform of length N = 2^a 3^b 5^c, in
+// application order: 8 while 8 divides what remains, then 6, 4, 2, 3 or 5.
+__host__ __device__ constexpr int dif_next(int rem) {
+  return rem % 8 == 0 ? 8 : rem % 6 == 0 ? 6 : rem % 4 == 0 ? 4 : rem % 2 == 0 ? 2 : rem % 3 == 0 ? 3 : 5;
+}
+__host__ __device__ constexpr int dif_radix(int N, int s) {
+  int rem = N;
+  for (int i = 0; i < s; ++i) rem /= dif_next(rem);
+  return dif_next(rem);
+}
+__host__ __device__ constexpr int dif_stages(int N) {
+  int s = 0;
+  for (int rem = N; rem > 1; rem /= dif_next(rem)) ++s;
+  return s;
+}
+__host__ __device__ constexpr int dif_block(int N, int s) {
+  int b = N;
+  for (int i = 0; i < s; ++i) b /= dif_radix(N, i);
+  return b;
+}
+__device__ __forceinline__ void dft_r(float2* v, int r) {
+  if (r == 8) dft8(v);
+  else if (r == 6) dft6(v);
+  else butterfly(v, r);
+}
+
+// Position of frequency f in the output of the in-place DIF transform (mixed-radix digit
+// reversal: stage s leaves digit k'_s of f = k'_0 + r_0 (k'_1 + r_1 (...)) at stride M_s).
+template <int N>
+__device__ __forceinline__ int dif_position(int f) {
+  int p = 0, block = N;
 #pragma unroll
-        for (int q = 0; q < r; ++q) {
-          const float2 a = src[((k + m * q) * L + j) * ES];
-          v[q] = q == 0 ? a : cmulf(a, tw[j * q * m]);  // j q m < L r m = N
-        }
-        butterfly(v, r);
-        float2* dst = out + line * LS;
-#pragma unroll
-        for (int q = 0; q < r; ++q) dst[(k * Ls + j + q * L) * ES] = v[q];
-      }
-      __syncthreads();
-      return StockhamStages<N, Ls, NL, LS, ES, LINE_FAST>::run(out, in, tw);
-    }
+  for (int s = 0; s < dif_stages(N); ++s) {
+    const int r = dif_radix(N, s);
+    block /= r;
+    p += (f % r) * block;
+    f /= r;
   }
+  return p;
+}
+
+// In-place forward DFT of L lines of length N held in shared memory as xs[i * L + line]
+// (lines fastest, so a warp touches whole 128-byte rows at every stage), by mixed-radix
+// decimation in frequency: stage s transforms groups {base + M k} with a radix-r DFT and
+// multiplies output k' by exp(-2 pi i j k' / B) (B = M r the stage's block, j = base mod M).
+// The result for frequency f sits at position dif_position<N>(f).  `pre` may rewrite the
+// first stage's inputs (pre(v, base, M, line) with v[k] = x[base + M k]).  All threads of the
+// block call it; it ends with __syncthreads().
+struct DifNoPre {
+  template <int R>
+  __device__ __forceinline__ void operator()(float2 (&)[R], int, int, int) const {}
 };
 
-// Forward DFT of NL lines of length N (all threads of the block call it; it synchronises
-// internally).  Returns the buffer holding the result.
-template <int N, int NL, int LS, int ES, bool LINE_FAST>
-__device__ __forceinline__ float2* smem_fft(float2* b0, float2* b1, const float2* __restrict__ tw) {
-  return StockhamStages<N, 1, NL, LS, ES, LINE_FAST>::run(b0, b1, tw);
+template <int N, int L, int S, class Pre>
+__device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
+                                               const float2* __restrict__ tw, const Pre& pre) {
+  if constexpr (S < dif_stages(N)) {
+    constexpr int r = dif_radix(N, S);
+    constexpr int B = dif_block(N, S);
+    constexpr int M = B / r;
+    for (int e = threadIdx.x; e < L * (N / r); e += blockDim.x) {
+      const int line = e % L, gi = e / L;
+      const int j = gi % M, base = (gi / M) * B + j;
+      float2 v[r];
+#pragma unroll
+      for (int k = 0; k < r; ++k) v[k] = xs[(base + M * k) * L + line];
+      if constexpr (S == 0) pre(v, base, M, line);
+      dft_r(v, r);
+      if constexpr (M > 1) {
+#pragma unroll
+        for (int k = 1; k < r; ++k) v[k] = cmulf(v[k], tw[(N / B) * j * k]);
+      }
+#pragma unroll
+      for (int k = 0; k < r; ++k) xs[(base + M * k) * L + line] = v[k];
+    }
+    __syncthreads();
+    dif_lines_from<N, L, S + 1>(xs, tw, pre);
+  }
+}
+template <int N, int L, class Pre = DifNoPre>
+__device__ __forceinline__ void dif_lines(float2* __restrict__ xs, const float2* __restrict__ tw,
+                                          const Pre& pre = Pre()) {
+  dif_lines_from<N, L, 0>(xs, tw, pre);
+}
+
+// tw[n] = exp(-2 pi i n / N), n < N (all threads of the block; no barrier).
+template <int N>
+__device__ __forceinline__ void dif_twiddles(float2* tw) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    float sn, cn;
+    sincospif(-2.0f * (float)i / (float)N, &sn, &cn);
+    tw[i] = make_float2(cn, sn);
+  }
 }
 
 // Lengths with compiled transform passes (2,3,5-smooth multiples of 16).

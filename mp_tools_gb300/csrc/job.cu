@@ -364,106 +364,184 @@ __global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
 //      weights, cs(t, Q)
 // K = 2h+1; frequency f is stored at index f + h.
 
-// Pass X: R contiguous rows of length N per CTA, one grid per blockIdx.y.
-template <int N, int R>
+// All three passes keep a tile of 16 (X, Y) or 2 x 16 (Z) lines of length N in shared memory
+// as [position][line] (lines fastest, so every warp access covers whole 128-byte rows), issue
+// all of a thread's global loads before storing any, transform in place (dif_lines) and read
+// the kept frequencies at their digit-reversed positions.
+constexpr int kPassLines = 16;
+
+template <int N>
+__device__ __forceinline__ void copy_twiddles(float2* tw, const float2* __restrict__ gtw) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[i];
+}
+__device__ __forceinline__ int wrap_freq(int f, int n) { return f < 0 ? f + n : f; }
+
+// Pass X: 16 contiguous rows of length N per CTA (one grid per blockIdx.y).  Rows are read 32
+// bytes (4 complex) per thread and transposed into the tile; the K0 kept frequencies of each
+// row are gathered into registers, staged as [row][K0] and stored as one contiguous block.
+template <int N>
 __global__ void __launch_bounds__(256)
-    fftx_prune_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
-                      const float2* __restrict__ tw, int h0, int K0, float2* __restrict__ b1) {
+    fftx_dif_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
+                    const float2* __restrict__ gtw, int h0, int K0, float2* __restrict__ b1) {
+  constexpr int L = kPassLines, NQ = N / 4;
+  constexpr int LOADS = (L * NQ + 255) / 256;          // quads per thread
+  constexpr int OUTS = (L * (N / 2 + 1) + 255) / 256;  // kept values per thread (K0 <= N/2+1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* s0 = reinterpret_cast<float2*>(smem_raw);
-  float2* s1 = s0 + R * N;
-  const int g = blockIdx.y;
-  const int row0 = blockIdx.x * R;
-  const float4* src = reinterpret_cast<const float4*>(fine + (int64_t)g * n_fine + (int64_t)row0 * N);
-  const int rows = min(R, n_rows - row0);
-  for (int e = threadIdx.x; e < R * N / 2; e += blockDim.x) {  // two complex per load
-    const int line = e / (N / 2);
-    const float4 v = line < rows ? src[e] : make_float4(0.f, 0.f, 0.f, 0.f);
-    s0[2 * e] = make_float2(v.x, v.y);
-    s0[2 * e + 1] = make_float2(v.z, v.w);
+  float2* xs = reinterpret_cast<float2*>(smem_raw);    // [N][L], then [L][K0]
+  float2* tw = xs + N * L;
+  const int tid = threadIdx.x, g = blockIdx.y;
+  const int row0 = blockIdx.x * L;
+  const int rows = min(L, n_rows - row0);
+  copy_twiddles<N>(tw, gtw);
+  const float2* src = fine + (int64_t)g * n_fine + (int64_t)row0 * N;
+  float4 va[LOADS], vb[LOADS];
+#pragma unroll
+  for (int p = 0; p < LOADS; ++p) {
+    const int e = tid + 256 * p;
+    const int r = e % L, xq = e / L;
+    va[p] = vb[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (e < L * NQ && r < rows) {
+      const float4* s4 = reinterpret_cast<const float4*>(src + (int64_t)r * N + 4 * xq);
+      va[p] = __ldcs(s4);
+      vb[p] = __ldcs(s4 + 1);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < LOADS; ++p) {
+    const int e = tid + 256 * p;
+    if (e < L * NQ) {
+      const int r = e % L, x = 4 * (e / L);
+      xs[(x + 0) * L + r] = make_float2(va[p].x, va[p].y);
+      xs[(x + 1) * L + r] = make_float2(va[p].z, va[p].w);
+      xs[(x + 2) * L + r] = make_float2(vb[p].x, vb[p].y);
+      xs[(x + 3) * L + r] = make_float2(vb[p].z, vb[p].w);
+    }
   }
   __syncthreads();
-  const float2* res = smem_fft<N, R, N, 1, false>(s0, s1, tw);
-  float2* dst = b1 + ((int64_t)g * n_rows + row0) * K0;
-  for (int e = threadIdx.x; e < rows * K0; e += blockDim.x) {
-    const int line = e / K0, i = e - line * K0;
-    const int f = i - h0;
-    dst[e] = res[line * N + (f < 0 ? f + N : f)];
+  dif_lines<N, L>(xs, tw);
+  float2 o[OUTS];
+#pragma unroll
+  for (int p = 0; p < OUTS; ++p) {
+    const int e = tid + 256 * p;
+    o[p] = make_float2(0.f, 0.f);
+    if (e < L * K0) o[p] = xs[dif_position<N>(wrap_freq(e / L - h0, N)) * L + e % L];
   }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < OUTS; ++p) {
+    const int e = tid + 256 * p;
+    if (e < L * K0) xs[(e % L) * K0 + e / L] = o[p];
+  }
+  __syncthreads();
+  float2* dst = b1 + ((int64_t)g * n_rows + row0) * K0;
+  for (int e = tid; e < rows * K0; e += 256) dst[e] = xs[e];
 }
 
-// Pass Y: a tile of T consecutive x-columns (length N along y) of one z-plane per CTA.
-template <int N, int T>
+// Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA.
+template <int N>
 __global__ void __launch_bounds__(256)
-    ffty_prune_kernel(const float2* __restrict__ b1, int n2, int K0,
-                      const float2* __restrict__ tw, int h1, int K1, float2* __restrict__ b2) {
+    ffty_dif_kernel(const float2* __restrict__ b1, int n2, int K0, const float2* __restrict__ gtw,
+                    int h1, int K1, float2* __restrict__ b2) {
+  constexpr int L = kPassLines;
+  constexpr int LOADS = (L * N + 255) / 256, BATCH = LOADS < 16 ? LOADS : 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* s0 = reinterpret_cast<float2*>(smem_raw);
-  float2* s1 = s0 + T * N;
-  const int x0 = blockIdx.x * T, z = blockIdx.y, g = blockIdx.z;
-  const float2* src = b1 + ((int64_t)g * n2 + z) * N * K0;
-  for (int e = threadIdx.x; e < N * T; e += blockDim.x) {
-    const int y = e / T, c = e - y * T;
-    const int x = x0 + c;
-    s0[e] = x < K0 ? src[(int64_t)y * K0 + x] : make_float2(0.f, 0.f);
+  float2* xs = reinterpret_cast<float2*>(smem_raw);    // [N][L]
+  float2* tw = xs + N * L;
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * L, z = blockIdx.y, g = blockIdx.z;
+  copy_twiddles<N>(tw, gtw);
+  const float2* src = b1 + ((int64_t)g * n2 + z) * (int64_t)N * K0;
+  for (int b0 = 0; b0 < LOADS; b0 += BATCH) {
+    float2 v[BATCH];
+#pragma unroll
+    for (int p = 0; p < BATCH; ++p) {
+      const int e = tid + 256 * (b0 + p);
+      const int c = e % L, y = e / L;
+      v[p] = make_float2(0.f, 0.f);
+      if (b0 + p < LOADS && e < L * N && x0 + c < K0) v[p] = __ldcs(src + (int64_t)y * K0 + x0 + c);
+    }
+#pragma unroll
+    for (int p = 0; p < BATCH; ++p) {
+      const int e = tid + 256 * (b0 + p);
+      if (b0 + p < LOADS && e < L * N) xs[e] = v[p];
+    }
   }
   __syncthreads();
-  const float2* res = smem_fft<N, T, 1, T, true>(s0, s1, tw);
-  float2* dst = b2 + ((int64_t)g * n2 + z) * K1 * K0;
-  for (int e = threadIdx.x; e < K1 * T; e += blockDim.x) {
-    const int i = e / T, c = e - i * T;
+  dif_lines<N, L>(xs, tw);
+  float2* dst = b2 + ((int64_t)g * n2 + z) * (int64_t)K1 * K0;
+  for (int e = tid; e < L * K1; e += 256) {
+    const int c = e % L, i = e / L;
     const int x = x0 + c;
     if (x >= K0) continue;
-    const int f = i - h1;
-    dst[(int64_t)i * K0 + x] = res[(f < 0 ? f + N : f) * T + c];
+    dst[(int64_t)i * K0 + x] = xs[dif_position<N>(wrap_freq(i - h1, N)) * L + c];
   }
 }
 
 // Pass Z fused with the deconvolution: CTA (x-tile, ky index iy) loads, for every grid, the T
 // z-columns (iy, x0..x0+T) and their mirrors (2h1-iy, 2h0-x), transforms all 2T lines, and
-// accumulates the weighted species amplitudes of the T x m2 output modes.
-template <int N, int T>
+// accumulates the weighted species amplitudes of its T x m2 output modes in registers.
+template <int N>
+__host__ __device__ constexpr int zpass_cols() { return N <= 512 ? 16 : 8; }
+
+template <int N>
 __global__ void __launch_bounds__(256)
-    fftz_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
-                       int h0, int h1, int h2, int ngroups, const float2* __restrict__ tw,
-                       const float* __restrict__ c0, const float* __restrict__ c1,
-                       const float* __restrict__ c2, WeightArgs w, float2* __restrict__ cs_frame,
-                       float2* __restrict__ cs_species_frame) {
+    fftz_dif_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
+                           int h0, int h1, int h2, int ngroups, const float2* __restrict__ gtw,
+                           const float* __restrict__ c0, const float* __restrict__ c1,
+                           const float* __restrict__ c2, WeightArgs w,
+                           float2* __restrict__ cs_frame, float2* __restrict__ cs_species_frame) {
+  constexpr int T = zpass_cols<N>(), L = 2 * T;
+  constexpr int LOADS = (L * N + 255) / 256, BATCH = LOADS < 16 ? LOADS : 16;
+  constexpr int OUTS = (T * (N / 2) + 255) / 256;       // m2 <= N/2 output z-modes
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NL = 2 * T;
-  float2* s0 = reinterpret_cast<float2*>(smem_raw);
-  float2* s1 = s0 + NL * N;
-  float2* acc = s1 + NL * N;  // [m2][T]
+  float2* xs = reinterpret_cast<float2*>(smem_raw);     // [N][L]: T columns, then T mirrors
+  float2* tw = xs + N * L;
+  const int tid = threadIdx.x;
   const int x0 = blockIdx.x * T, iy = blockIdx.y;
   const int iym = 2 * h1 - iy;
   const int64_t nm = (int64_t)m0 * m1 * m2;
-  for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
+  copy_twiddles<N>(tw, gtw);
+  float2 acc[OUTS];
+#pragma unroll
+  for (int p = 0; p < OUTS; ++p) acc[p] = make_float2(0.f, 0.f);
   const float cy = c1[iy];
   const int ky = iy - h1;
   for (int g = 0; g < ngroups; ++g) {
     const float2* src = b2 + (int64_t)g * N * K1 * K0;
     const int pair = w.pair[g];
-    for (int e = threadIdx.x; e < N * NL; e += blockDim.x) {
-      const int z = e / NL, l = e - z * NL;
-      const int c = l < T ? l : l - T;
-      const int x = x0 + c;
-      float2 v = make_float2(0.f, 0.f);
-      if (x < m0 && (l < T || pair)) {
-        const int xi = l < T ? x : 2 * h0 - x;
-        const int yi = l < T ? iy : iym;
-        v = src[((int64_t)z * K1 + yi) * K0 + xi];
+    if (g > 0) __syncthreads();  // the previous group's reads of the tile are complete
+    for (int b0 = 0; b0 < LOADS; b0 += BATCH) {
+      float2 v[BATCH];
+#pragma unroll
+      for (int p = 0; p < BATCH; ++p) {
+        const int e = tid + 256 * (b0 + p);
+        const int l = e % L, z = e / L;
+        const int c = l < T ? l : l - T;
+        const int x = x0 + c;
+        v[p] = make_float2(0.f, 0.f);
+        if (b0 + p < LOADS && e < L * N && x < m0 && (l < T || pair)) {
+          const int xi = l < T ? x : 2 * h0 - x;
+          const int yi = l < T ? iy : iym;
+          v[p] = __ldcs(src + ((int64_t)z * K1 + yi) * K0 + xi);
+        }
       }
-      s0[e] = v;
+#pragma unroll
+      for (int p = 0; p < BATCH; ++p) {
+        const int e = tid + 256 * (b0 + p);
+        if (b0 + p < LOADS && e < L * N) xs[e] = v[p];
+      }
     }
     __syncthreads();
-    const float2* res = smem_fft<N, NL, 1, NL, true>(s0, s1, tw);
+    dif_lines<N, L>(xs, tw);
     const int sa = w.sp_a[g], sb = w.sp_b[g];
-    for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) {
-      const int iz = e / T, c = e - iz * T;
+#pragma unroll
+    for (int p = 0; p < OUTS; ++p) {
+      const int e = tid + 256 * p;
+      const int c = e % T, iz = e / T;
       const int x = x0 + c;
-      if (x >= m0) continue;
+      if (iz >= m2 || x >= m0) continue;
       const int fz = iz - h2;
-      const float2 G = res[(fz < 0 ? fz + N : fz) * NL + c];
+      const float2 G = xs[dif_position<N>(wrap_freq(fz, N)) * L + c];
       const float corr = c0[x] * cy * c2[iz];
       const int kx = x - h0, kz = fz;
       float s2 = 0.f;
@@ -474,44 +552,36 @@ __global__ void __launch_bounds__(256)
           qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
         s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
       }
-      float2 a = acc[e];
       const int64_t q = ((int64_t)iz * m1 + iy) * m0 + x;
       if (pair) {
-        const int mz = -fz;
-        const float2 Gm = res[(mz < 0 ? mz + N : mz) * NL + T + c];
+        const float2 Gm = xs[dif_position<N>(wrap_freq(-fz, N)) * L + T + c];
         const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
         const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
         const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
-        a.x += wa * ar + wb * br;
-        a.y += wa * ai + wb * bi;
+        acc[p].x += wa * ar + wb * br;
+        acc[p].y += wa * ai + wb * bi;
         if (w.store_species) {
           cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
           cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
         }
       } else {
         const float wa = species_weight<float>(w, sa, s2);
-        a.x += wa * G.x * corr;
-        a.y += wa * G.y * corr;
+        acc[p].x += wa * G.x * corr;
+        acc[p].y += wa * G.y * corr;
         if (w.store_species)
           cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
       }
-      acc[e] = a;
     }
-    __syncthreads();
   }
-  for (int e = threadIdx.x; e < m2 * T; e += blockDim.x) {
-    const int iz = e / T, c = e - iz * T;
+#pragma unroll
+  for (int p = 0; p < OUTS; ++p) {
+    const int e = tid + 256 * p;
+    const int c = e % T, iz = e / T;
     const int x = x0 + c;
-    if (x >= m0) continue;
-    const float2 a = acc[e];
-    cs_frame[((int64_t)iz * m1 + iy) * m0 + x] = make_float2(a.x * w.wnorm_f, a.y * w.wnorm_f);
+    if (iz >= m2 || x >= m0) continue;
+    cs_frame[((int64_t)iz * m1 + iy) * m0 + x] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
   }
 }
-
-// Tile sizes per transform length (shared memory: X 16*R*N, Y 16*T*N, Z 32*T*N + 8*T*m2 bytes)
-constexpr int prune_rx(int n) { return n <= 512 ? 8 : 4; }
-constexpr int prune_ty(int n) { return n <= 512 ? 8 : 4; }
-constexpr int prune_tz(int n) { return n <= 512 ? 4 : 2; }
 
 struct PruneLaunch {
   const float2* fine;
@@ -526,32 +596,36 @@ struct PruneLaunch {
 };
 
 template <int N>
+static size_t pass_smem(int lines) {
+  return (size_t)N * lines * sizeof(float2) + (size_t)N * sizeof(float2);
+}
+
+template <int N>
 static int launch_prune_x(const PruneLaunch& p) {
-  constexpr int R = prune_rx(N);
   const int n_rows = p.n[1] * p.n[2];
-  const size_t sm = (size_t)16 * R * N;
-  cudaFuncSetAttribute(fftx_prune_kernel<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  fftx_prune_kernel<N, R><<<dim3((unsigned)((n_rows + R - 1) / R), (unsigned)p.ngrid), 256, sm, p.s>>>(
-      p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
+  const size_t sm = pass_smem<N>(kPassLines);
+  cudaFuncSetAttribute(fftx_dif_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  fftx_dif_kernel<N><<<dim3((unsigned)((n_rows + kPassLines - 1) / kPassLines), (unsigned)p.ngrid),
+                       256, sm, p.s>>>(p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
 template <int N>
 static int launch_prune_y(const PruneLaunch& p) {
-  constexpr int T = prune_ty(N);
-  const size_t sm = (size_t)16 * T * N;
-  cudaFuncSetAttribute(ffty_prune_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  ffty_prune_kernel<N, T><<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)p.n[2], (unsigned)p.ngrid),
-                            256, sm, p.s>>>(p.b1, p.n[2], p.K[0], p.tw[1], p.h[1], p.K[1], p.b2);
+  const size_t sm = pass_smem<N>(kPassLines);
+  cudaFuncSetAttribute(ffty_dif_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  ffty_dif_kernel<N><<<dim3((unsigned)((p.K[0] + kPassLines - 1) / kPassLines), (unsigned)p.n[2],
+                            (unsigned)p.ngrid),
+                       256, sm, p.s>>>(p.b1, p.n[2], p.K[0], p.tw[1], p.h[1], p.K[1], p.b2);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
 template <int N>
 static int launch_prune_z(const PruneLaunch& p, const WeightArgs& w, float2* csf, float2* css) {
-  constexpr int T = prune_tz(N);
-  const size_t sm = (size_t)32 * T * N + (size_t)8 * T * p.m[2];
-  cudaFuncSetAttribute(fftz_deconv_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  fftz_deconv_kernel<N, T><<<dim3((unsigned)((p.m[0] + T - 1) / T), (unsigned)p.m[1]), 256, sm, p.s>>>(
+  constexpr int T = zpass_cols<N>();
+  const size_t sm = pass_smem<N>(2 * T);
+  cudaFuncSetAttribute(fftz_dif_deconv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  fftz_dif_deconv_kernel<N><<<dim3((unsigned)((p.m[0] + T - 1) / T), (unsigned)p.m[1]), 256, sm, p.s>>>(
       p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.h[0], p.h[1], p.h[2], p.ngroups, p.tw[2],
       p.c[0], p.c[1], p.c[2], w, csf, css);
   MPSQ_LAUNCH_CHECK();
@@ -877,16 +951,23 @@ extern "C" int mpsq_job_destroy(mpsq_job* j) {
   return MPSQ_OK;
 }
 
-extern "C" int mpsq_job_set_frames(mpsq_job* j, const float* pos, int32_t first, int32_t count,
-                                   int host) {
+extern "C" int mpsq_job_set_frames_on(mpsq_job* j, const float* pos, int32_t first,
+                                      int32_t count, int host, void* stream) {
   if (!j || !pos) return fail(MPSQ_ERR_ARG, "set_frames: null pointer");
   if (first < 0 || count < 0 || first + count > j->d.n_frames)
     return fail(MPSQ_ERR_ARG, "set_frames: frames [%d, %d) outside [0, %d)", first, first + count,
                 j->d.n_frames);
   const size_t bytes = (size_t)count * j->d.n_atoms_frame * sizeof(float4);
   float4* dst = j->traj + (size_t)first * j->d.n_atoms_frame;
-  MPSQ_CUDA_TRY(cudaMemcpyAsync(dst, pos, bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, j->s));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(dst, pos, bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                (cudaStream_t)stream));
   return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_set_frames(mpsq_job* j, const float* pos, int32_t first, int32_t count,
+                                   int host) {
+  if (!j) return fail(MPSQ_ERR_ARG, "set_frames: null job");
+  return mpsq_job_set_frames_on(j, pos, first, count, host, j->s);
 }
 
 extern "C" int mpsq_job_set_cell_index(mpsq_job* j, const int32_t* at_ind, int host) {

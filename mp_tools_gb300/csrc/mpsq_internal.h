@@ -283,6 +283,14 @@ int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,
                   typename Cplx<T>::type* fine, cudaStream_t s);
 
+// Tensor-core spreading of packed real species pairs (3D, 16^3 tiles, FP32 grid); strengths
+// must be real with |s| <= 8.  Selected by default; MPSQ_SPREAD=fma in the environment keeps
+// the CUDA-core kernel instead.
+bool spread_pair_mma_enabled();
+int launch_spread_pair_mma(const SpreadArgs& a, const RecF* recs, const int* idx,
+                           const float2* cv, int64_t c_stride, const int* starts, int nkeys,
+                           int ntrans, float2* fine, cudaStream_t s);
+
 // cuFFT plan cache key
 int make_fft_plan(const GridGeom& g, int ngrid, int precision, cudaStream_t s, cufftHandle* h);
 int exec_fft(cufftHandle h, int precision, void* data, int direction);

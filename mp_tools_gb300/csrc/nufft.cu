@@ -515,6 +515,8 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
                               typename Cplx<T>::type* fine, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value && DIM == 3) {
     if (a.tile[0] == 16 && a.tile[1] == 16 && a.tile[2] == 16 && a.w >= 3 && a.w <= 8) {
+      if (real_pair && spread_pair_mma_enabled())
+        return launch_spread_pair_mma(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
       dim3 grid((unsigned)nkeys, (unsigned)ntrans);
       const int rp = real_pair ? 1 : 0;
       switch (a.w) {

@@ -1,0 +1,322 @@
+// Tensor-core spreading of packed real species pairs (3D, FP32 results).
+//
+// Within one 16^3 tile the spread of the tile's point records onto z-plane p is a small
+// matrix product
+//     G_p[y, x] = sum_k A_p[y, k] B[k, x],   A_p[y, k] = s_k ky_k[y] kz_k[p],   B[k, x] = kx_k[x]
+// over the records k (kx, ky, kz: the ES kernel values of record k along each axis, zero
+// outside its w-cell support; s_k its real strength).  A record adds into the real part of the
+// grid when it belongs to the first species of the pair and into the imaginary part otherwise
+// (the pair is separated after the transform by Hermitian symmetry), so the two components
+// are two independent products over disjoint record sets.
+//
+// The products run on the tensor cores as mma.sync m16n8k16 (f16 operands, FP32
+// accumulators).  FP32 accuracy is kept by splitting each operand v into two f16 terms:
+// hi = v with its 13 low mantissa bits cleared (exact in f16), lo = v - hi (exact in FP32,
+// rounded to f16), and accumulating Ah*Bh + Ah*Bl + Al*Bh; the dropped Al*Bl term and the
+// rounding of lo are below 2^-21 of each product.  A and B carry a factor 2^10 so that the lo
+// terms of kernel values down to ~1e-4 stay in the f16 normal range; the tile is scaled by
+// 2^-20 when it is written.  Strengths must satisfy |s| <= 8 (the spatial Hann window's
+// maximum), which keeps |A| <= 2^13 well inside the f16 range.
+//
+// Organisation (one CTA = one tile, 8 warps, warp w owns z-planes 2w and 2w+1):
+//  * records are staged in chunks of up to 240; each chunk is counting-sorted in shared
+//    memory by (component, start z) and laid out as K-blocks of 16 records that share one
+//    component (the second component's block starts on a multiple of 16); thread t then
+//    evaluates the kernel of the record in slot t, so a warp writes consecutive columns;
+//  * a warp skips every plane outside the union of a K-block's z-supports (sorted start z
+//    makes that union narrow);
+//  * the accumulators stay in registers; every cell of the tile is written once at the end
+//    with 16-byte stores (no zero fill, no global atomics).
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "mpsq_internal.h"
+
+namespace mpsq {
+namespace {
+
+constexpr int kCh = 256;            // staging slots per chunk
+constexpr int kCap = kCh - 16;      // records per chunk (room for the alignment gap)
+constexpr int kKp = kCh + 8;        // float row pitch: conflict-free 64-bit fragment loads
+constexpr int kKh = kCh / 2 + 4;    // f16-pair row pitch: conflict-free 32-bit fragment loads
+
+template <int W>
+struct MmaSmem {
+  static constexpr int kKeys = W + 15;   // start z in [-(W-1), 15]
+  float ky[16][kKp];                     // s * ky * 2^10, row y, column slot
+  float kz[16][kKp];                     // kz, row z
+  uint32_t kxh[16][kKh];                 // hi(kx * 2^10) as f16 pairs (slots 2j, 2j+1), row x
+  uint32_t kxl[16][kKh];                 // lo(kx * 2^10)
+  int lz[kCh];                           // start z of the record in each slot
+  RecF rec[kCh];                         // the record sorted into each slot
+  float str[kCh];                        // its real strength
+  int count[2 * kKeys];
+  int base[2 * kKeys];
+  int n0, b1, n1;
+};
+
+__device__ __forceinline__ float es_value(float z, float beta) {
+  return expf(beta * (sqrtf(fmaxf(1.0f - z * z, 0.0f)) - 1.0f));
+}
+
+__device__ __forceinline__ float clear_low13(float v) {
+  return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ uint32_t pack_f16x2(float first, float second) {
+  const __half2 h = __floats2half2_rn(first, second);   // first -> low 16 bits
+  uint32_t u;
+  memcpy(&u, &h, sizeof(u));
+  return u;
+}
+
+__device__ __forceinline__ void mma_16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
+                                          uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One component's K-blocks [kb0, kb1) of the staged chunk into acc[plane][n-tile][4].
+template <int W>
+__device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb1, int end,
+                                           int p0, int g, int t, float (&acc)[2][2][4]) {
+  for (int kb = kb0; kb < kb1; ++kb) {
+    const int first = kb * 16;
+    const int last = min(first + 15, end - 1);
+    const int zlo = sm.lz[first], zhi = sm.lz[last] + W - 1;
+    const bool use0 = p0 >= zlo && p0 <= zhi;
+    const bool use1 = p0 + 1 >= zlo && p0 + 1 <= zhi;
+    if (!use0 && !use1) continue;                       // warp-uniform
+    uint32_t bh[2][2], bl[2][2];
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      bh[nt][0] = sm.kxh[nt * 8 + g][kb * 8 + t];
+      bh[nt][1] = sm.kxh[nt * 8 + g][kb * 8 + 4 + t];
+      bl[nt][0] = sm.kxl[nt * 8 + g][kb * 8 + t];
+      bl[nt][1] = sm.kxl[nt * 8 + g][kb * 8 + 4 + t];
+    }
+    const float2 yA0 = *reinterpret_cast<const float2*>(&sm.ky[g][first + 2 * t]);
+    const float2 yA1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t]);
+    const float2 yB0 = *reinterpret_cast<const float2*>(&sm.ky[g][first + 2 * t + 8]);
+    const float2 yB1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t + 8]);
+#pragma unroll
+    for (int pi = 0; pi < 2; ++pi) {
+      if (!(pi ? use1 : use0)) continue;
+      const int p = p0 + pi;
+      const float2 zA = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t]);
+      const float2 zB = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t + 8]);
+      // fragment order: (row g, k 2t..2t+1), (row g+8, same), (row g, k 2t+8..), (row g+8, ..)
+      const float a[8] = {yA0.x * zA.x, yA0.y * zA.y, yA1.x * zA.x, yA1.y * zA.y,
+                          yB0.x * zB.x, yB0.y * zB.y, yB1.x * zB.x, yB1.y * zB.y};
+      uint32_t ah[4], al[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float h0 = clear_low13(a[2 * j]), h1 = clear_low13(a[2 * j + 1]);
+        ah[j] = pack_f16x2(h0, h1);
+        al[j] = pack_f16x2(a[2 * j] - h0, a[2 * j + 1] - h1);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        mma_16816(acc[pi][nt], al, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[pi][nt], ah, bl[nt][0], bl[nt][1]);
+        mma_16816(acc[pi][nt], ah, bh[nt][0], bh[nt][1]);
+      }
+    }
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256, 3)
+    spread3_pair_mma_kernel(SpreadArgs a, const RecF* __restrict__ recs,
+                            const int* __restrict__ idx, const float2* __restrict__ cv,
+                            int64_t c_stride, const int* __restrict__ starts,
+                            float2* __restrict__ fine) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MmaSmem<W>& sm = *reinterpret_cast<MmaSmem<W>*>(smem_raw);
+  constexpr int K1 = MmaSmem<W>::kKeys;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int p0 = 2 * warp;
+  const int64_t key = blockIdx.x;
+  const int trans = blockIdx.y;
+  const int keygrid = (int)(key / a.n_tiles);
+  const int tile = (int)(key - (int64_t)keygrid * a.n_tiles);
+  const int tx = tile % a.ntile[0];
+  const int ty = (tile / a.ntile[0]) % a.ntile[1];
+  const int tz = tile / (a.ntile[0] * a.ntile[1]);
+  float acc_re[2][2][4], acc_im[2][2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc_re[i][j][k] = acc_im[i][j][k] = 0.0f;
+  const float beta = (float)a.beta;
+  const float s2w = 2.0f / (float)W;
+  const int r0 = starts[key], r1 = starts[key + 1];
+  for (int c0 = r0; c0 < r1; c0 += kCap) {
+    const int n = min(kCap, r1 - c0);
+    {  // zero the staging arrays (alignment-gap slots and out-of-support rows must read 0)
+      uint4* z4 = reinterpret_cast<uint4*>(&sm.ky[0][0]);
+      constexpr int nz = (int)((sizeof(sm.ky) + sizeof(sm.kz) + sizeof(sm.kxh) + sizeof(sm.kxl)) / 16);
+      for (int e = tid; e < nz; e += 256) z4[e] = make_uint4(0u, 0u, 0u, 0u);
+      for (int e = tid; e < 2 * K1; e += 256) sm.count[e] = 0;
+    }
+    __syncthreads();
+    // 1. rank every record within its (component, start z) key
+    RecF rec;
+    float sv = 0.0f;
+    int k = 0, rank = 0;
+    if (tid < n) {
+      const int r = c0 + tid;
+      rec = recs[r];
+      sv = (idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r]).x;
+      const int lz = ((rec.packed >> 16) & 0xff) - 64;
+      const int comp = (rec.packed >> 24) & 1;
+      k = comp * K1 + min(max(lz + W - 1, 0), K1 - 1);
+      rank = atomicAdd(&sm.count[k], 1);
+    }
+    __syncthreads();
+    // 2. exclusive scan of the key counts (one warp; K1 <= 23 keys per component); the
+    //    second component starts on a multiple of 16
+    if (warp == 0) {
+      const int c0n = lane < K1 ? sm.count[lane] : 0;
+      const int c1n = lane < K1 ? sm.count[K1 + lane] : 0;
+      int i0 = c0n, i1 = c1n;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u0 = __shfl_up_sync(0xffffffffu, i0, o), u1 = __shfl_up_sync(0xffffffffu, i1, o);
+        if (lane >= o) {
+          i0 += u0;
+          i1 += u1;
+        }
+      }
+      const int n0 = __shfl_sync(0xffffffffu, i0, 31), n1 = __shfl_sync(0xffffffffu, i1, 31);
+      const int b1 = (n0 + 15) & ~15;
+      if (lane < K1) {
+        sm.base[lane] = i0 - c0n;
+        sm.base[K1 + lane] = b1 + i1 - c1n;
+      }
+      if (lane == 0) {
+        sm.n0 = n0;
+        sm.b1 = b1;
+        sm.n1 = n1;
+      }
+    }
+    __syncthreads();
+    // 3. place each record in its sorted slot
+    if (tid < n) {
+      const int slot = sm.base[k] + rank;
+      sm.rec[slot] = rec;
+      sm.str[slot] = sv;
+    }
+    __syncthreads();
+    // 4. thread t evaluates the kernel of the record in slot t and writes its support rows
+    //    (consecutive threads write consecutive columns of a row: no bank conflicts)
+    {
+      const int st = tid;
+      const bool live = st < sm.n0 || (st >= sm.b1 && st < sm.b1 + sm.n1);
+      if (live) {
+        const RecF q = sm.rec[st];
+        const float s = sm.str[st] * 1024.0f;
+        const int lx = (q.packed & 0xff) - 64;
+        const int ly = ((q.packed >> 8) & 0xff) - 64;
+        const int lz = ((q.packed >> 16) & 0xff) - 64;
+        __half* xh = reinterpret_cast<__half*>(&sm.kxh[0][0]);
+        __half* xl = reinterpret_cast<__half*>(&sm.kxl[0][0]);
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+          const int x = lx + i, y = ly + i, z = lz + i;
+          if (x >= 0 && x < 16) {
+            const float v = es_value((q.dx + (float)i) * s2w, beta) * 1024.0f;
+            const float h = clear_low13(v);
+            xh[x * 2 * kKh + st] = __float2half_rn(h);
+            xl[x * 2 * kKh + st] = __float2half_rn(v - h);
+          }
+          if (y >= 0 && y < 16) sm.ky[y][st] = es_value((q.dy + (float)i) * s2w, beta) * s;
+          if (z >= 0 && z < 16) sm.kz[z][st] = es_value((q.dz + (float)i) * s2w, beta);
+        }
+        sm.lz[st] = lz;
+      }
+    }
+    __syncthreads();
+    const int n0 = sm.n0, b1 = sm.b1, n1 = sm.n1;
+    mma_region<W>(sm, 0, (n0 + 15) >> 4, n0, p0, g, t, acc_re);
+    mma_region<W>(sm, b1 >> 4, (b1 + n1 + 15) >> 4, b1 + n1, p0, g, t, acc_im);
+    __syncthreads();
+  }
+  float2* out = fine + (int64_t)(keygrid + trans) * a.n_fine;
+  const int64_t nf0 = a.nf[0], nf1 = a.nf[1];
+  const float sc = 1.0f / 1048576.0f;
+#pragma unroll
+  for (int pi = 0; pi < 2; ++pi) {
+    const int64_t zrow = ((int64_t)tz * 16 + p0 + pi) * nf1 + (int64_t)ty * 16;
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      const int64_t xcol = (int64_t)tx * 16 + nt * 8 + 2 * t;
+#pragma unroll
+      for (int hv = 0; hv < 2; ++hv) {
+        const int y = g + 8 * hv;
+        const float4 v = make_float4(acc_re[pi][nt][2 * hv] * sc, acc_im[pi][nt][2 * hv] * sc,
+                                     acc_re[pi][nt][2 * hv + 1] * sc, acc_im[pi][nt][2 * hv + 1] * sc);
+        *reinterpret_cast<float4*>(out + (zrow + y) * nf0 + xcol) = v;
+      }
+    }
+  }
+}
+
+template <int W>
+int launch_w(const SpreadArgs& a, const RecF* recs, const int* idx, const float2* cv,
+             int64_t c_stride, const int* starts, int nkeys, int ntrans, float2* fine,
+             cudaStream_t s) {
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(spread3_pair_mma_kernel<W>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(MmaSmem<W>));
+  });
+  if (attr != cudaSuccess) return fail(MPSQ_ERR_CUDA, "spread mma attribute: %s", cudaGetErrorString(attr));
+  spread3_pair_mma_kernel<W><<<dim3((unsigned)nkeys, (unsigned)ntrans), 256, sizeof(MmaSmem<W>), s>>>(
+      a, recs, idx, cv, c_stride, starts, fine);
+  MPSQ_LAUNCH_CHECK();
+  return MPSQ_OK;
+}
+
+}  // namespace
+
+bool spread_pair_mma_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("MPSQ_SPREAD");
+    return !(e && strcmp(e, "fma") == 0);
+  }();
+  return on;
+}
+
+int launch_spread_pair_mma(const SpreadArgs& a, const RecF* recs, const int* idx,
+                           const float2* cv, int64_t c_stride, const int* starts, int nkeys,
+                           int ntrans, float2* fine, cudaStream_t s) {
+  if (a.dim != 3 || a.tile[0] != 16 || a.tile[1] != 16 || a.tile[2] != 16)
+    return fail(MPSQ_ERR_ARG, "spread mma: 16^3 tiles only");
+  if ((reinterpret_cast<uintptr_t>(fine) & 15) != 0 || (a.nf[0] & 1) != 0)
+    return fail(MPSQ_ERR_ARG, "spread mma: grid must be 16-byte aligned with even rows");
+  switch (a.w) {
+    case 3: return launch_w<3>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 4: return launch_w<4>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 5: return launch_w<5>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 6: return launch_w<6>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 7: return launch_w<7>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 8: return launch_w<8>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    default: return fail(MPSQ_ERR_ARG, "spread mma: kernel width %d not compiled", a.w);
+  }
+}
+
+}  // namespace mpsq

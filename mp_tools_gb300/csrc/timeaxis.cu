@@ -11,6 +11,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fft_smem.cuh"
 #include "mpsq_internal.h"
 
 namespace mpsq {
@@ -302,6 +303,121 @@ __global__ void gauss_fft_kernel(const typename Cplx<T>::type* __restrict__ cs, 
   }
 }
 
+// FP32 Gaussian-window spectrum with an in-place mixed-radix (8, then 4 or 2) decimation-in-
+// frequency FFT.  One CTA holds the N x 16 tile cs(t, q0..q0+15) (one 128-byte line per time
+// row, three CTAs per SM for N = 512); every thread issues all its N/32 loads before using
+// them.  The elastic mean is subtracted and the window applied in the first stage; the
+// spectrum is read back at the digit-reversed positions.
+constexpr int kGaussQ = 16;
+
+// First-stage hook: subtract the column's elastic mean and apply the time window.
+struct GaussPre {
+  const float* gw;
+  const float2* mean;
+  template <int R>
+  __device__ __forceinline__ void operator()(float2 (&v)[R], int base, int M, int line) const {
+    const float2 m = mean[line];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const float g = gw[base + M * k];
+      v[k] = make_float2((v[k].x - m.x) * g, (v[k].y - m.y) * g);
+    }
+  }
+};
+
+template <int N>
+__global__ void __launch_bounds__(256)
+    gauss_dif_kernel(const float2* __restrict__ cs, int64_t nq, const float* __restrict__ gwin,
+                     int n_freq, const float* __restrict__ q2n, float scale,
+                     float* __restrict__ out) {
+  constexpr int QT = kGaussQ, RL = N / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* xs = reinterpret_cast<float2*>(smem_raw);       // [N][QT]
+  float2* tw = xs + N * QT;                                 // exp(-2 pi i n / N)
+  float4* part = reinterpret_cast<float4*>(tw + N);         // [8 warps][8 column pairs]
+  float2* mean = reinterpret_cast<float2*>(part + 64);      // [QT]
+  float* gw = reinterpret_cast<float*>(mean + QT);          // [N]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t q0 = (int64_t)blockIdx.x * QT;
+  dif_twiddles<N>(tw);
+  for (int i = tid; i < N; i += blockDim.x) gw[i] = gwin[i];
+  // rows t = (tid >> 3) + 32 i, columns q0 + 2 (tid & 7) + {0, 1}
+  const int c2 = tid & 7, r0 = tid >> 3;
+  const int64_t qa = q0 + 2 * c2;
+  float4 v[RL];
+  if ((nq & 1) == 0) {           // rows start on 16-byte boundaries: one float4 per pair
+#pragma unroll
+    for (int i = 0; i < RL; ++i) {
+      const int64_t t = r0 + 32 * i;
+      v[i] = qa < nq ? __ldcs(reinterpret_cast<const float4*>(cs + t * nq + qa))
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < RL; ++i) {
+      const int64_t t = r0 + 32 * i;
+      const float2 a = qa < nq ? __ldcs(cs + t * nq + qa) : make_float2(0.f, 0.f);
+      const float2 b = qa + 1 < nq ? __ldcs(cs + t * nq + qa + 1) : make_float2(0.f, 0.f);
+      v[i] = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < RL; ++i) {
+    s.x += v[i].x; s.y += v[i].y; s.z += v[i].z; s.w += v[i].w;
+    *reinterpret_cast<float4*>(&xs[(r0 + 32 * i) * QT + 2 * c2]) = v[i];
+  }
+  // column sums: lanes c2, c2+8, c2+16, c2+24 of a warp, then the 8 warps
+#pragma unroll
+  for (int o = 8; o < 32; o <<= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    s.z += __shfl_xor_sync(0xffffffffu, s.z, o);
+    s.w += __shfl_xor_sync(0xffffffffu, s.w, o);
+  }
+  if (lane < 8) part[warp * 8 + lane] = s;
+  __syncthreads();
+  if (tid < QT) {
+    float mr = 0.f, mi = 0.f;
+    for (int w = 0; w < 8; ++w) {
+      const float4 p = part[w * 8 + (tid >> 1)];
+      mr += (tid & 1) ? p.z : p.x;
+      mi += (tid & 1) ? p.w : p.y;
+    }
+    mean[tid] = make_float2(mr / (float)N, mi / (float)N);
+  }
+  __syncthreads();
+  dif_lines<N, QT>(xs, tw, GaussPre{gw, mean});
+  for (int e = tid; e < n_freq * QT; e += blockDim.x) {
+    const int q = e % QT, f = e / QT;
+    const int64_t qq = q0 + q;
+    if (qq >= nq) continue;
+    const float2 X = xs[dif_position<N>(f) * QT + q];
+    float val = (X.x * X.x + X.y * X.y) * scale;
+    if (q2n) {
+      const float w = q2n[qq];
+      val *= w * w;
+    }
+    out[(int64_t)f * nq + qq] = val;
+  }
+}
+
+template <int N>
+static size_t gauss_dif_smem() {
+  return (size_t)N * kGaussQ * sizeof(float2) + (size_t)N * sizeof(float2) + 64 * sizeof(float4) +
+         kGaussQ * sizeof(float2) + (size_t)N * sizeof(float);
+}
+
+template <int N>
+static int launch_gauss_dif(const float2* cs, int64_t nq, const float* gwin, int n_freq,
+                            const float* q2n, float scale, float* out, cudaStream_t s) {
+  const size_t smem = gauss_dif_smem<N>();
+  cudaFuncSetAttribute(gauss_dif_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const unsigned nb = (unsigned)((nq + kGaussQ - 1) / kGaussQ);
+  gauss_dif_kernel<N><<<nb, 256, smem, s>>>(cs, nq, gwin, n_freq, q2n, scale, out);
+  return MPSQ_OK;
+}
+
 // ------------------------------------------------------------------------------- host
 static int tile_cols(int nt, size_t csz, size_t extra, size_t limit) {
   int qt = 32;
@@ -494,6 +610,16 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
     cudaFuncSetAttribute(gauss_fft_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     gauss_fft_kernel<double><<<nb, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, nt, logn, QT, dg,
                                                     n_freq, dq, scale, b.dev);
+  } else if (nt >= 64) {
+    const float2* cs = (const float2*)v.cs;
+    const float sc = (float)scale;
+    switch (nt) {
+      case 64: launch_gauss_dif<64>(cs, v.n_q, dg, n_freq, dq, sc, b.dev, v.s); break;
+      case 128: launch_gauss_dif<128>(cs, v.n_q, dg, n_freq, dq, sc, b.dev, v.s); break;
+      case 256: launch_gauss_dif<256>(cs, v.n_q, dg, n_freq, dq, sc, b.dev, v.s); break;
+      case 512: launch_gauss_dif<512>(cs, v.n_q, dg, n_freq, dq, sc, b.dev, v.s); break;
+      default: launch_gauss_dif<1024>(cs, v.n_q, dg, n_freq, dq, sc, b.dev, v.s); break;
+    }
   } else {
     cudaFuncSetAttribute(gauss_fft_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     gauss_fft_kernel<float><<<nb, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, nt, logn, QT, dg,

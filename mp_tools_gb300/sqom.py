@@ -255,6 +255,8 @@ class SqomJob:
         self.n_atoms_frame = d.n_atoms_frame
         self.precision = precision
         self._h = C.c_void_p()
+        self._stream = int(stream or 0)
+        self._copy_stream = None
         check(L.mpsq_job_create(C.byref(d), C.c_void_p(stream or 0), C.byref(self._h)), "job_create")
 
     # ------------------------------------------------------------------ lifecycle
@@ -283,9 +285,15 @@ class SqomJob:
 
     # ------------------------------------------------------------------ inputs
     def set_frames(self, pos, first: int = 0):
-        """pos: (count, n_atoms_frame, 4) float32, numpy (host) or torch CUDA tensor."""
-        host = not (hasattr(pos, "is_cuda") and pos.is_cuda)
-        if host:
+        """pos: (count, n_atoms_frame, 4) float32 — numpy array, torch CPU tensor (pinned memory
+        is copied by DMA without staging) or torch CUDA tensor."""
+        if hasattr(pos, "is_cuda"):          # torch tensor: use its own buffer, no host copy
+            import torch
+            if pos.dtype != torch.float32 or not pos.is_contiguous():
+                pos = pos.to(torch.float32).contiguous()
+            host = not pos.is_cuda
+        else:
+            host = True
             pos = np.ascontiguousarray(pos, dtype=np.float32)
         count = pos.shape[0] if pos.ndim == 3 else 1
         if pos.shape[-2] != self.n_atoms_frame or pos.shape[-1] != 4:
@@ -300,6 +308,45 @@ class SqomJob:
         self.sync()
 
     # ------------------------------------------------------------------ compute
+    def transform_from_host(self, frames, chunk: int = 32):
+        """Uploads host frames (count = n_frames; a pinned torch CPU tensor copies by DMA) in
+        chunks of `chunk` frames on a second CUDA stream and transforms every chunk on the
+        job's stream as soon as it has arrived, so the upload of chunk c+1 overlaps the
+        transform of chunk c.  Uploads start after all work already queued on the job's
+        stream, which may still read the previous trajectory."""
+        import torch
+        if hasattr(frames, "is_cuda"):
+            if frames.is_cuda:
+                raise ValueError("transform_from_host takes host frames")
+            if frames.dtype != torch.float32 or not frames.is_contiguous():
+                frames = frames.to(torch.float32).contiguous()
+            base = frames.data_ptr()
+        else:
+            frames = np.ascontiguousarray(frames, dtype=np.float32)
+            base = frames.ctypes.data
+        F = frames.shape[0]
+        if F != self.n_frames or frames.shape[1] != self.n_atoms_frame:
+            raise ValueError("frames must be (n_frames, n_atoms_frame, 4)")
+        L = _lib.load()
+        job_stream = (torch.cuda.ExternalStream(self._stream) if self._stream
+                      else torch.cuda.default_stream())
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream()
+        cs = self._copy_stream
+        tail = torch.cuda.Event()
+        tail.record(job_stream)
+        cs.wait_event(tail)
+        frame_bytes = self.n_atoms_frame * 16
+        for c0 in range(0, F, chunk):
+            n = min(chunk, F - c0)
+            check(L.mpsq_job_set_frames_on(self._h, C.c_void_p(base + c0 * frame_bytes), c0, n, 1,
+                                           C.c_void_p(cs.cuda_stream)), "set_frames_on")
+            ev = torch.cuda.Event()
+            ev.record(cs)
+            job_stream.wait_event(ev)
+            self.transform(c0, n)
+        self._keep = frames
+
     def transform(self, first: int = 0, count: int | None = None):
         count = self.n_frames - first if count is None else count
         check(_lib.load().mpsq_job_transform(self._h, first, count), "transform")

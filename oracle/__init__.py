@@ -10,11 +10,20 @@ Contents
     C/OpenMP, scipy/pocketfft FFT, deconvolution by quadrature of the kernel transform), the
     stand-in for FINUFFT+OpenMP, which is not available on either machine.
   * ``sqom_ref`` — numpy restatement of the mp_sqom loops around the NUFFT call.
+  * ``sql_ref`` — numpy restatement of mp_sql's spherical average (Q cube, FP32 |Q| binning,
+    normalisation, smoothing, X-ray output modes).
 
-Parity status: parity unpinned for the mp_sqom path — its golden outputs in the reference tree
-(examples/single_crystal_BZO/bzo200d_sq_*.txt) need frame files that are absent, and the
-reference itself (Fortran + FINUFFT) cannot be built on these machines.  The functions here
-are checked against known-answer identities (tests/test_oracle.py).
+Parity status
+  * Pinned on the reference's own outputs: ``es_nufft`` + ``sql_ref`` reproduce the four mp_sql
+    result tables of the reference's amorphous Al92U8 example (examples/amorphous_Al92U08,
+    files _40.._43: Z(Q), I(Q), S(Q), unscaled I(Q), total and partial columns) from the
+    example's own input frame, within 7e-7 of each column's maximum for Q <= 7.9 A^-1
+    (tests/test_golden_alu.py).  This pins the type-1 transform itself (the same finufft2d1
+    boundary mp_sqom calls), its mode order and sign, and the radial post-processing.
+  * The mp_sqom-specific loops (selection, phases, species weights, time windows) have no
+    runnable golden output in the reference tree (its BZO map files need frame files that
+    are absent; only three map rows serve as a text-format check); they are checked against
+    known-answer identities (tests/test_oracle.py) and the reference's formulas line by line.
 """
 from __future__ import annotations
 

@@ -1,0 +1,150 @@
+"""GPU parity of the FP32 fast paths that the small-system job tests do not reach:
+the mixed-radix Gaussian-window spectrum (64..1024 frames, even and odd Q counts, with and
+without the 1/|Q| factor) and the tensor-core spreading of packed species pairs (against the
+CUDA-core spreading kernel, selected with MPSQ_SPREAD=fma in a child process, and against
+the FP64 direct sum)."""
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_l2
+from mp_tools_gb300 import _lib, sql
+from mp_tools_gb300.sqom import QGrid, SqomJob
+from oracle import sqom_ref
+
+pytestmark = pytest.mark.gpu
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def random_walk(n_atoms, F, box, seed, sigma=0.05):
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(-box / 2, box / 2, (n_atoms, 3))
+    fr = np.empty((F, n_atoms, 4), np.float32)
+    for t in range(F):
+        fr[t, :, :3] = p
+        fr[t, :, 3] = 0.0
+        p = p + rng.normal(0, sigma, p.shape)
+    return fr
+
+
+@pytest.mark.parametrize("F", [64, 128, 256, 512, 1024])
+@pytest.mark.parametrize("grid_kind", ["even", "odd"])
+def test_gauss_spectrum_long_runs(cuda, F, grid_kind):
+    if grid_kind == "even":      # 8^3 = 512 modes: 16-byte rows, float4 loads
+        grid = QGrid(_lib.CELL, (4, 4, 4), n_bz=2, a_par=(4.19,) * 3, ndim=3)
+        box = 4.0
+        frames = random_walk(60, F, box, seed=F, sigma=0.01)
+    else:                        # 13^3 = 2197 modes: odd row length, float2 loads, ragged tile
+        grid = sql.SqlGrid(4.0, (10.0,) * 3)
+        frames = random_walk(60, F, 10.0, seed=F + 1)
+    counts = [40, 20]
+    job = SqomJob(grid, species_counts=counts, n_frames=F, precision=_lib.FP32, eps=1e-6,
+                  n_atoms_frame=frames.shape[1])
+    try:
+        job.set_frames(frames)
+        job.transform()
+        job.sync()
+        cs = job.amplitudes().astype(np.complex128)
+        rng = np.random.default_rng(5)
+        q2 = rng.uniform(0.5, 2.0, grid.n_modes).astype(np.float32)
+        for fwhm, n_freq, qn in ((F / 2, F // 2 + 1, None), (F / 8, F // 4, q2)):
+            got = job.sqw_gauss(fwhm_frames=fwhm, n_freq=n_freq, q2_norm=qn, normalize=False)
+            g = sqom_ref.gauss_window(F, fwhm)
+            want = sqom_ref.gauss_spectrum(cs, fwhm, n_freq, None if qn is None else qn.astype(np.float64),
+                                           1.0 / g.sum())
+            assert got.shape == want.shape
+            assert rel_l2(got, want) < 2e-5, (F, grid_kind, fwhm)
+    finally:
+        job.close()
+
+
+def _alloy(n_atoms=6000, F=2, box=30.0, seed=3):
+    rng = np.random.default_rng(seed)
+    fr = np.zeros((F, n_atoms, 4), np.float32)
+    fr[:, :, :3] = rng.uniform(-box / 2, box / 2, (n_atoms, 3))
+    fr[1:, :, :3] += rng.normal(0, 0.2, (F - 1, n_atoms, 3)).astype(np.float32)
+    return fr, [int(n_atoms * 0.92), n_atoms - int(n_atoms * 0.92)]
+
+
+_CHILD = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests")
+import test_kernels_gpu as T
+from mp_tools_gb300 import _lib, sql
+fr, counts = T._alloy()
+grid = sql.SqlGrid(5.0, (30.0,) * 3)
+job = T.SqomJob(grid, species_counts=counts, n_frames=fr.shape[0], precision=_lib.FP32, eps=1e-6,
+                store_species=True, n_atoms_frame=fr.shape[1])
+job.set_frames(fr); job.transform(); job.sync()
+np.save(sys.argv[2], job.amplitudes())
+job.close()
+"""
+
+
+def test_tensor_core_spread_matches_cuda_core_spread(cuda, tmp_path):
+    """Packed Al/U pair job (both species in one grid) through the default (tensor-core)
+    spread and, in a child process with MPSQ_SPREAD=fma, through the CUDA-core spread."""
+    out = {}
+    for mode in ("mma", "fma"):
+        env = dict(os.environ)
+        if mode == "fma":
+            env["MPSQ_SPREAD"] = "fma"
+        else:
+            env.pop("MPSQ_SPREAD", None)
+        path = tmp_path / f"cs_{mode}.npy"
+        subprocess.run([sys.executable, "-c", _CHILD, str(ROOT), str(path)], check=True, env=env,
+                       timeout=600)
+        out[mode] = np.load(path)
+    assert out["mma"].shape == out["fma"].shape
+    assert rel_l2(out["mma"], out["fma"]) < 2e-6
+
+
+def test_tensor_core_spread_against_direct_sum(cuda):
+    fr, counts = _alloy()
+    grid = sql.SqlGrid(5.0, (30.0,) * 3)
+    job = SqomJob(grid, species_counts=counts, n_frames=fr.shape[0], precision=_lib.FP32,
+                  eps=1e-6, n_atoms_frame=fr.shape[1])
+    try:
+        job.set_frames(fr)
+        job.transform()
+        job.sync()
+        cs = job.amplitudes()
+    finally:
+        job.close()
+    n = grid.n_q[0]
+    d = grid.d_q.astype(np.float64)
+    for t in range(fr.shape[0]):
+        r = fr[t, :, :3].astype(np.float64)
+        want = oracle.dirft3d1(r[:, 0] * d[0], r[:, 1] * d[1], r[:, 2] * d[2], np.ones(len(r)),
+                               -1, n, n, n)
+        assert rel_l2(cs[t], want.reshape(-1)) < 1e-5
+
+
+def test_transform_from_host_equals_device_upload(cuda):
+    """Chunked upload on a second stream (pinned host tensor) gives bit-identical amplitudes
+    to one upload followed by the transform, also when the job is run twice back to back."""
+    import torch
+    fr, counts = _alloy(n_atoms=3000, F=40)
+    grid = sql.SqlGrid(4.0, (30.0,) * 3)
+    kw = dict(species_counts=counts, n_frames=fr.shape[0], precision=_lib.FP32, eps=1e-6,
+              n_atoms_frame=fr.shape[1])
+    a = SqomJob(grid, **kw)
+    b = SqomJob(grid, **kw)
+    try:
+        a.set_frames(fr)
+        a.transform()
+        a.sync()
+        pinned = torch.from_numpy(fr).pin_memory()
+        for _ in range(2):
+            b.transform_from_host(pinned, chunk=7)
+        b.sync()
+        assert np.array_equal(a.amplitudes(), b.amplitudes())
+    finally:
+        a.close()
+        b.close()
