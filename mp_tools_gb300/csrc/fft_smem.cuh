@@ -167,28 +167,45 @@ __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
     constexpr int r = dif_radix(N, S);
     constexpr int B = dif_block(N, S);
     constexpr int M = B / r;
-    for (int e = threadIdx.x; e < L * (N / r); e += blockDim.x) {
-      const int line = e % L, gi = e / L;
+    constexpr int LP = L / 2;      // a thread transforms two adjacent lines (16-byte accesses)
+    for (int e = threadIdx.x; e < LP * (N / r); e += blockDim.x) {
+      const int lp = e % LP, gi = e / LP;
       const int j = gi % M, base = (gi / M) * B + j;
-      float2 v[r];
+      float2 va[r], vb[r];
 #pragma unroll
-      for (int k = 0; k < r; ++k) v[k] = xs[(base + M * k) * L + line];
-      if constexpr (S == 0) pre(v, base, M, line);
-      dft_r(v, r);
+      for (int k = 0; k < r; ++k) {
+        const float4 q = *reinterpret_cast<const float4*>(&xs[(base + M * k) * L + 2 * lp]);
+        va[k] = make_float2(q.x, q.y);
+        vb[k] = make_float2(q.z, q.w);
+      }
+      if constexpr (S == 0) {
+        pre(va, base, M, 2 * lp);
+        pre(vb, base, M, 2 * lp + 1);
+      }
+      dft_r(va, r);
+      dft_r(vb, r);
       if constexpr (M > 1) {
 #pragma unroll
-        for (int k = 1; k < r; ++k) v[k] = cmulf(v[k], tw[(N / B) * j * k]);
+        for (int k = 1; k < r; ++k) {
+          const float2 w = tw[(N / B) * j * k];
+          va[k] = cmulf(va[k], w);
+          vb[k] = cmulf(vb[k], w);
+        }
       }
 #pragma unroll
-      for (int k = 0; k < r; ++k) xs[(base + M * k) * L + line] = v[k];
+      for (int k = 0; k < r; ++k)
+        *reinterpret_cast<float4*>(&xs[(base + M * k) * L + 2 * lp]) =
+            make_float4(va[k].x, va[k].y, vb[k].x, vb[k].y);
     }
     __syncthreads();
     dif_lines_from<N, L, S + 1>(xs, tw, pre);
   }
 }
+// L must be even; xs must be 16-byte aligned.
 template <int N, int L, class Pre = DifNoPre>
 __device__ __forceinline__ void dif_lines(float2* __restrict__ xs, const float2* __restrict__ tw,
                                           const Pre& pre = Pre()) {
+  static_assert(L % 2 == 0, "dif_lines transforms lines in pairs");
   dif_lines_from<N, L, 0>(xs, tw, pre);
 }
 

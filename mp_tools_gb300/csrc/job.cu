@@ -376,16 +376,17 @@ __device__ __forceinline__ void copy_twiddles(float2* tw, const float2* __restri
 }
 __device__ __forceinline__ int wrap_freq(int f, int n) { return f < 0 ? f + n : f; }
 
-// Pass X: 16 contiguous rows of length N per CTA (one grid per blockIdx.y).  Rows are read 32
-// bytes (4 complex) per thread and transposed into the tile; the K0 kept frequencies of each
-// row are gathered into registers, staged as [row][K0] and stored as one contiguous block.
+// Pass X: 16 contiguous rows of length N per CTA (one grid per blockIdx.y).  A thread reads two
+// adjacent complex of two adjacent rows (16 bytes each) and stores them as two 16-byte row
+// pairs of the tile; the K0 kept frequencies of each row pair are gathered into registers,
+// staged as [row][K0] and stored as one contiguous block.
 template <int N>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
     fftx_dif_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
                     const float2* __restrict__ gtw, int h0, int K0, float2* __restrict__ b1) {
-  constexpr int L = kPassLines, NQ = N / 4;
-  constexpr int LOADS = (L * NQ + 255) / 256;          // quads per thread
-  constexpr int OUTS = (L * (N / 2 + 1) + 255) / 256;  // kept values per thread (K0 <= N/2+1)
+  constexpr int L = kPassLines, LP = L / 2, NP = N / 2;
+  constexpr int LOADS = (LP * NP + 255) / 256;          // (row pair, x pair) items per thread
+  constexpr int OUTS = (LP * (N / 2 + 1) + 255) / 256;  // kept row-pair values (K0 <= N/2+1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);    // [N][L], then [L][K0]
   float2* tw = xs + N * L;
@@ -398,52 +399,55 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int p = 0; p < LOADS; ++p) {
     const int e = tid + 256 * p;
-    const int r = e % L, xq = e / L;
+    const int rp = e % LP, xp = e / LP;
     va[p] = vb[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (e < L * NQ && r < rows) {
-      const float4* s4 = reinterpret_cast<const float4*>(src + (int64_t)r * N + 4 * xq);
-      va[p] = __ldcs(s4);
-      vb[p] = __ldcs(s4 + 1);
+    if (e < LP * NP) {
+      if (2 * rp < rows) va[p] = __ldcs(reinterpret_cast<const float4*>(src + (int64_t)(2 * rp) * N + 2 * xp));
+      if (2 * rp + 1 < rows) vb[p] = __ldcs(reinterpret_cast<const float4*>(src + (int64_t)(2 * rp + 1) * N + 2 * xp));
     }
   }
 #pragma unroll
   for (int p = 0; p < LOADS; ++p) {
     const int e = tid + 256 * p;
-    if (e < L * NQ) {
-      const int r = e % L, x = 4 * (e / L);
-      xs[(x + 0) * L + r] = make_float2(va[p].x, va[p].y);
-      xs[(x + 1) * L + r] = make_float2(va[p].z, va[p].w);
-      xs[(x + 2) * L + r] = make_float2(vb[p].x, vb[p].y);
-      xs[(x + 3) * L + r] = make_float2(vb[p].z, vb[p].w);
+    if (e < LP * NP) {
+      const int rp = e % LP, x = 2 * (e / LP);
+      *reinterpret_cast<float4*>(&xs[x * L + 2 * rp]) = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
+      *reinterpret_cast<float4*>(&xs[(x + 1) * L + 2 * rp]) = make_float4(va[p].z, va[p].w, vb[p].z, vb[p].w);
     }
   }
   __syncthreads();
   dif_lines<N, L>(xs, tw);
-  float2 o[OUTS];
+  float4 o[OUTS];
 #pragma unroll
   for (int p = 0; p < OUTS; ++p) {
     const int e = tid + 256 * p;
-    o[p] = make_float2(0.f, 0.f);
-    if (e < L * K0) o[p] = xs[dif_position<N>(wrap_freq(e / L - h0, N)) * L + e % L];
+    o[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (e < LP * K0)
+      o[p] = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(e / LP - h0, N)) * L + 2 * (e % LP)]);
   }
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < OUTS; ++p) {
     const int e = tid + 256 * p;
-    if (e < L * K0) xs[(e % L) * K0 + e / L] = o[p];
+    if (e < LP * K0) {
+      const int r = 2 * (e % LP), i = e / LP;
+      xs[r * K0 + i] = make_float2(o[p].x, o[p].y);
+      xs[(r + 1) * K0 + i] = make_float2(o[p].z, o[p].w);
+    }
   }
   __syncthreads();
   float2* dst = b1 + ((int64_t)g * n_rows + row0) * K0;
   for (int e = tid; e < rows * K0; e += 256) dst[e] = xs[e];
 }
 
-// Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA.
+// Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA; a thread moves
+// two adjacent columns.
 template <int N>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
     ffty_dif_kernel(const float2* __restrict__ b1, int n2, int K0, const float2* __restrict__ gtw,
                     int h1, int K1, float2* __restrict__ b2) {
-  constexpr int L = kPassLines;
-  constexpr int LOADS = (L * N + 255) / 256, BATCH = LOADS < 16 ? LOADS : 16;
+  constexpr int L = kPassLines, LP = L / 2;
+  constexpr int LOADS = (LP * N + 255) / 256, BATCH = LOADS < 8 ? LOADS : 8;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);    // [N][L]
   float2* tw = xs + N * L;
@@ -452,47 +456,56 @@ __global__ void __launch_bounds__(256)
   copy_twiddles<N>(tw, gtw);
   const float2* src = b1 + ((int64_t)g * n2 + z) * (int64_t)N * K0;
   for (int b0 = 0; b0 < LOADS; b0 += BATCH) {
-    float2 v[BATCH];
+    float2 va[BATCH], vb[BATCH];
 #pragma unroll
     for (int p = 0; p < BATCH; ++p) {
       const int e = tid + 256 * (b0 + p);
-      const int c = e % L, y = e / L;
-      v[p] = make_float2(0.f, 0.f);
-      if (b0 + p < LOADS && e < L * N && x0 + c < K0) v[p] = __ldcs(src + (int64_t)y * K0 + x0 + c);
+      const int x = x0 + 2 * (e % LP), y = e / LP;
+      va[p] = vb[p] = make_float2(0.f, 0.f);
+      if (b0 + p < LOADS && e < LP * N) {
+        const float2* q = src + (int64_t)y * K0 + x;
+        if (x < K0) va[p] = __ldcs(q);
+        if (x + 1 < K0) vb[p] = __ldcs(q + 1);
+      }
     }
 #pragma unroll
     for (int p = 0; p < BATCH; ++p) {
       const int e = tid + 256 * (b0 + p);
-      if (b0 + p < LOADS && e < L * N) xs[e] = v[p];
+      if (b0 + p < LOADS && e < LP * N)
+        *reinterpret_cast<float4*>(&xs[2 * e]) = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
     }
   }
   __syncthreads();
   dif_lines<N, L>(xs, tw);
   float2* dst = b2 + ((int64_t)g * n2 + z) * (int64_t)K1 * K0;
-  for (int e = tid; e < L * K1; e += 256) {
-    const int c = e % L, i = e / L;
+  for (int e = tid; e < LP * K1; e += 256) {
+    const int c = 2 * (e % LP), i = e / LP;
     const int x = x0 + c;
     if (x >= K0) continue;
-    dst[(int64_t)i * K0 + x] = xs[dif_position<N>(wrap_freq(i - h1, N)) * L + c];
+    const float4 v = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(i - h1, N)) * L + c]);
+    float2* q = dst + (int64_t)i * K0 + x;
+    q[0] = make_float2(v.x, v.y);
+    if (x + 1 < K0) q[1] = make_float2(v.z, v.w);
   }
 }
 
 // Pass Z fused with the deconvolution: CTA (x-tile, ky index iy) loads, for every grid, the T
 // z-columns (iy, x0..x0+T) and their mirrors (2h1-iy, 2h0-x), transforms all 2T lines, and
-// accumulates the weighted species amplitudes of its T x m2 output modes in registers.
+// accumulates the weighted species amplitudes of its T x m2 output modes in registers (two
+// adjacent columns per thread).
 template <int N>
-__host__ __device__ constexpr int zpass_cols() { return N <= 512 ? 16 : 8; }
+__host__ __device__ constexpr int zpass_cols() { return 8; }
 
 template <int N>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
     fftz_dif_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
                            int h0, int h1, int h2, int ngroups, const float2* __restrict__ gtw,
                            const float* __restrict__ c0, const float* __restrict__ c1,
                            const float* __restrict__ c2, WeightArgs w,
                            float2* __restrict__ cs_frame, float2* __restrict__ cs_species_frame) {
-  constexpr int T = zpass_cols<N>(), L = 2 * T;
-  constexpr int LOADS = (L * N + 255) / 256, BATCH = LOADS < 16 ? LOADS : 16;
-  constexpr int OUTS = (T * (N / 2) + 255) / 256;       // m2 <= N/2 output z-modes
+  constexpr int T = zpass_cols<N>(), L = 2 * T, LP = L / 2, TP = T / 2;
+  constexpr int LOADS = (LP * N + 255) / 256, BATCH = LOADS < 8 ? LOADS : 8;
+  constexpr int OUTS = (TP * (N / 2) + 255) / 256;      // column pairs x m2 (m2 <= N/2)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);     // [N][L]: T columns, then T mirrors
   float2* tw = xs + N * L;
@@ -501,9 +514,9 @@ __global__ void __launch_bounds__(256)
   const int iym = 2 * h1 - iy;
   const int64_t nm = (int64_t)m0 * m1 * m2;
   copy_twiddles<N>(tw, gtw);
-  float2 acc[OUTS];
+  float4 acc[OUTS];
 #pragma unroll
-  for (int p = 0; p < OUTS; ++p) acc[p] = make_float2(0.f, 0.f);
+  for (int p = 0; p < OUTS; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
   const float cy = c1[iy];
   const int ky = iy - h1;
   for (int g = 0; g < ngroups; ++g) {
@@ -511,24 +524,26 @@ __global__ void __launch_bounds__(256)
     const int pair = w.pair[g];
     if (g > 0) __syncthreads();  // the previous group's reads of the tile are complete
     for (int b0 = 0; b0 < LOADS; b0 += BATCH) {
-      float2 v[BATCH];
+      float2 va[BATCH], vb[BATCH];
 #pragma unroll
       for (int p = 0; p < BATCH; ++p) {
         const int e = tid + 256 * (b0 + p);
-        const int l = e % L, z = e / L;
-        const int c = l < T ? l : l - T;
+        const int l = 2 * (e % LP), z = e / LP;
+        const bool mirror = l >= T;
+        const int c = mirror ? l - T : l;
         const int x = x0 + c;
-        v[p] = make_float2(0.f, 0.f);
-        if (b0 + p < LOADS && e < L * N && x < m0 && (l < T || pair)) {
-          const int xi = l < T ? x : 2 * h0 - x;
-          const int yi = l < T ? iy : iym;
-          v[p] = __ldcs(src + ((int64_t)z * K1 + yi) * K0 + xi);
+        va[p] = vb[p] = make_float2(0.f, 0.f);
+        if (b0 + p < LOADS && e < LP * N && (!mirror || pair)) {
+          const float2* row = src + ((int64_t)z * K1 + (mirror ? iym : iy)) * K0;
+          if (x < m0) va[p] = __ldcs(row + (mirror ? 2 * h0 - x : x));
+          if (x + 1 < m0) vb[p] = __ldcs(row + (mirror ? 2 * h0 - x - 1 : x + 1));
         }
       }
 #pragma unroll
       for (int p = 0; p < BATCH; ++p) {
         const int e = tid + 256 * (b0 + p);
-        if (b0 + p < LOADS && e < L * N) xs[e] = v[p];
+        if (b0 + p < LOADS && e < LP * N)
+          *reinterpret_cast<float4*>(&xs[2 * e]) = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
       }
     }
     __syncthreads();
@@ -537,49 +552,67 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int p = 0; p < OUTS; ++p) {
       const int e = tid + 256 * p;
-      const int c = e % T, iz = e / T;
-      const int x = x0 + c;
-      if (iz >= m2 || x >= m0) continue;
+      const int c = 2 * (e % TP), iz = e / TP;
+      if (iz >= m2 || x0 + c >= m0) continue;
       const int fz = iz - h2;
-      const float2 G = xs[dif_position<N>(wrap_freq(fz, N)) * L + c];
-      const float corr = c0[x] * cy * c2[iz];
-      const int kx = x - h0, kz = fz;
-      float s2 = 0.f;
-      if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
-        float qv[3];
+      const float4 G2 = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(fz, N)) * L + c]);
+      float4 Gm2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (pair) Gm2 = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(-fz, N)) * L + T + c]);
+      const int kz = fz;
 #pragma unroll
-        for (int b = 0; b < 3; ++b)
-          qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
-        s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
-      }
-      const int64_t q = ((int64_t)iz * m1 + iy) * m0 + x;
-      if (pair) {
-        const float2 Gm = xs[dif_position<N>(wrap_freq(-fz, N)) * L + T + c];
-        const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
-        const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
-        const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
-        acc[p].x += wa * ar + wb * br;
-        acc[p].y += wa * ai + wb * bi;
-        if (w.store_species) {
-          cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
-          cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
+      for (int hv = 0; hv < 2; ++hv) {
+        const int x = x0 + c + hv;
+        if (x >= m0) continue;
+        const float2 G = hv ? make_float2(G2.z, G2.w) : make_float2(G2.x, G2.y);
+        const float2 Gm = hv ? make_float2(Gm2.z, Gm2.w) : make_float2(Gm2.x, Gm2.y);
+        const float corr = c0[x] * cy * c2[iz];
+        const int kx = x - h0;
+        float s2 = 0.f;
+        if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+          float qv[3];
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
+          s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
         }
-      } else {
-        const float wa = species_weight<float>(w, sa, s2);
-        acc[p].x += wa * G.x * corr;
-        acc[p].y += wa * G.y * corr;
-        if (w.store_species)
-          cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
+        const int64_t q = ((int64_t)iz * m1 + iy) * m0 + x;
+        float ax, ay;
+        if (pair) {
+          const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
+          const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
+          const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
+          ax = wa * ar + wb * br;
+          ay = wa * ai + wb * bi;
+          if (w.store_species) {
+            cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
+            cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
+          }
+        } else {
+          const float wa = species_weight<float>(w, sa, s2);
+          ax = wa * G.x * corr;
+          ay = wa * G.y * corr;
+          if (w.store_species)
+            cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
+        }
+        if (hv) {
+          acc[p].z += ax;
+          acc[p].w += ay;
+        } else {
+          acc[p].x += ax;
+          acc[p].y += ay;
+        }
       }
     }
   }
 #pragma unroll
   for (int p = 0; p < OUTS; ++p) {
     const int e = tid + 256 * p;
-    const int c = e % T, iz = e / T;
+    const int c = 2 * (e % TP), iz = e / TP;
     const int x = x0 + c;
     if (iz >= m2 || x >= m0) continue;
-    cs_frame[((int64_t)iz * m1 + iy) * m0 + x] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
+    float2* q = cs_frame + ((int64_t)iz * m1 + iy) * m0 + x;
+    q[0] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
+    if (x + 1 < m0) q[1] = make_float2(acc[p].z * w.wnorm_f, acc[p].w * w.wnorm_f);
   }
 }
 

@@ -84,6 +84,24 @@ __device__ __forceinline__ void mma_16816(float (&c)[4], const uint32_t (&a)[4],
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// Split f16 A fragment (hi, lo) of plane p for the K-block starting at slot `first`:
+// rows g, g+8 (y) x columns 2t, 2t+1, 2t+8, 2t+9 (records), A = (s ky)[y] * kz[p].
+template <int W>
+__device__ __forceinline__ void build_a(const MmaSmem<W>& sm, int p, int first, int t,
+                                        float2 yA0, float2 yA1, float2 yB0, float2 yB1,
+                                        uint32_t (&ah)[4], uint32_t (&al)[4]) {
+  const float2 zA = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t]);
+  const float2 zB = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t + 8]);
+  const float a[8] = {yA0.x * zA.x, yA0.y * zA.y, yA1.x * zA.x, yA1.y * zA.y,
+                      yB0.x * zB.x, yB0.y * zB.y, yB1.x * zB.x, yB1.y * zB.y};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float h0 = clear_low13(a[2 * j]), h1 = clear_low13(a[2 * j + 1]);
+    ah[j] = pack_f16x2(h0, h1);
+    al[j] = pack_f16x2(a[2 * j] - h0, a[2 * j + 1] - h1);
+  }
+}
+
 // One component's K-blocks [kb0, kb1) of the staged chunk into acc[plane][n-tile][4].
 template <int W>
 __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb1, int end,
@@ -107,27 +125,36 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
     const float2 yA1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t]);
     const float2 yB0 = *reinterpret_cast<const float2*>(&sm.ky[g][first + 2 * t + 8]);
     const float2 yB1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t + 8]);
-#pragma unroll
-    for (int pi = 0; pi < 2; ++pi) {
-      if (!(pi ? use1 : use0)) continue;
-      const int p = p0 + pi;
-      const float2 zA = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t]);
-      const float2 zB = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t + 8]);
-      // fragment order: (row g, k 2t..2t+1), (row g+8, same), (row g, k 2t+8..), (row g+8, ..)
-      const float a[8] = {yA0.x * zA.x, yA0.y * zA.y, yA1.x * zA.x, yA1.y * zA.y,
-                          yB0.x * zB.x, yB0.y * zB.y, yB1.x * zB.x, yB1.y * zB.y};
-      uint32_t ah[4], al[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float h0 = clear_low13(a[2 * j]), h1 = clear_low13(a[2 * j + 1]);
-        ah[j] = pack_f16x2(h0, h1);
-        al[j] = pack_f16x2(a[2 * j] - h0, a[2 * j + 1] - h1);
-      }
+    if (use0 && use1) {   // both planes: four independent accumulator chains, interleaved
+      uint32_t ah0[4], al0[4], ah1[4], al1[4];
+      build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah0, al0);
+      build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah1, al1);
 #pragma unroll
       for (int nt = 0; nt < 2; ++nt) {
-        mma_16816(acc[pi][nt], al, bh[nt][0], bh[nt][1]);
-        mma_16816(acc[pi][nt], ah, bl[nt][0], bl[nt][1]);
-        mma_16816(acc[pi][nt], ah, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[0][nt], al0, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[1][nt], al1, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[0][nt], ah0, bl[nt][0], bl[nt][1]);
+        mma_16816(acc[1][nt], ah1, bl[nt][0], bl[nt][1]);
+        mma_16816(acc[0][nt], ah0, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[1][nt], ah1, bh[nt][0], bh[nt][1]);
+      }
+    } else if (use0) {
+      uint32_t ah[4], al[4];
+      build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah, al);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        mma_16816(acc[0][nt], al, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[0][nt], ah, bl[nt][0], bl[nt][1]);
+        mma_16816(acc[0][nt], ah, bh[nt][0], bh[nt][1]);
+      }
+    } else {
+      uint32_t ah[4], al[4];
+      build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah, al);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        mma_16816(acc[1][nt], al, bh[nt][0], bh[nt][1]);
+        mma_16816(acc[1][nt], ah, bl[nt][0], bl[nt][1]);
+        mma_16816(acc[1][nt], ah, bh[nt][0], bh[nt][1]);
       }
     }
   }

@@ -127,8 +127,10 @@ def test_tensor_core_spread_against_direct_sum(cuda):
 
 
 def test_transform_from_host_equals_device_upload(cuda):
-    """Chunked upload on a second stream (pinned host tensor) gives bit-identical amplitudes
-    to one upload followed by the transform, also when the job is run twice back to back."""
+    """Chunked upload on a second stream (pinned host tensor) gives the amplitudes of one upload
+    followed by the transform, also when the job is run twice back to back.  (Equal up to FP32
+    rounding: the order of records within a tile, and so of the sums, follows the binning's
+    atomics and is not fixed from run to run.)"""
     import torch
     fr, counts = _alloy(n_atoms=3000, F=40)
     grid = sql.SqlGrid(4.0, (30.0,) * 3)
@@ -144,7 +146,7 @@ def test_transform_from_host_equals_device_upload(cuda):
         for _ in range(2):
             b.transform_from_host(pinned, chunk=7)
         b.sync()
-        assert np.array_equal(a.amplitudes(), b.amplitudes())
+        assert rel_l2(b.amplitudes(), a.amplitudes()) < 1e-6
     finally:
         a.close()
         b.close()
