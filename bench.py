@@ -416,6 +416,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
+        cpu_port_frames(pos0, counts, box, grid, 1)  # thread pool / FFT warm-up, not timed
         el, pts, thr = cpu_port_frames(pos0, counts, box, grid, args.cpu_frames)
         cpu = {"value": pts / el, "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{args.cpu_frames} frame(s) x 2 species of the same workload, "

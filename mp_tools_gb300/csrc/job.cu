@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -133,6 +134,17 @@ struct mpsq_job {
   float2* tw[3] = {nullptr, nullptr, nullptr};
   float2* b1 = nullptr;
   int h[3] = {0, 0, 0}, K[3] = {1, 1, 1};
+  // second frame lane (pruned FP32 path): its own stream and per-frame scratch, so that two
+  // frames are in flight at once and their latency-bound kernels overlap
+  bool lane2 = false;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  void* fine2 = nullptr;
+  int* counts2 = nullptr;
+  int* starts2 = nullptr;
+  void* recs2 = nullptr;
+  void* str2 = nullptr;
+  float2* b1_2 = nullptr;
 };
 
 namespace mpsq {
@@ -759,6 +771,15 @@ static void job_free(mpsq_job* j) {
   cudaFree(j->err);
   cudaFree(j->b1);
   for (auto& t : j->tw) cudaFree(t);
+  cudaFree(j->fine2);
+  cudaFree(j->counts2);
+  cudaFree(j->starts2);
+  cudaFree(j->recs2);
+  cudaFree(j->str2);
+  cudaFree(j->b1_2);
+  if (j->fork) cudaEventDestroy(j->fork);
+  if (j->join) cudaEventDestroy(j->join);
+  if (j->s2) cudaStreamDestroy(j->s2);
   for (auto& e : j->ev)
     if (e) cudaEventDestroy(e);
   delete j;
@@ -781,7 +802,16 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
   b += (int64_t)d->n_frames * g.n_modes * (int64_t)csize(d->precision);     // cs(t,Q)
   if (d->store_species)
     b += (int64_t)d->n_frames * d->n_species * g.n_modes * (int64_t)csize(d->precision);
-  b += g.n_fine * (int64_t)csize(d->precision) / 4;  // cuFFT work area (estimate)
+  bool pruned = d->precision == MPSQ_FP32 && d->ndim == 3 && !d->no_pruned_fft;
+  for (int k = 0; k < 3 && pruned; ++k) pruned = fft_size_compiled((int)g.nf[k]);
+  if (pruned) {  // X-pass output, plus a second frame lane (fine grid, bins, records, X output)
+    const int64_t b1 = (int64_t)std::max(1, ng) * g.nf[2] * g.nf[1] * (2 * (g.m[0] / 2) + 1) * 8;
+    b += b1;
+    b += (int64_t)std::max(1, ng) * g.n_fine * 8 + (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8 +
+         d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision)) + b1;
+  } else {
+    b += g.n_fine * (int64_t)csize(d->precision) / 4;  // cuFFT work area (estimate)
+  }
   *bytes = b;
   return MPSQ_OK;
 }
@@ -948,7 +978,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
       j->h[k] = (int)(j->g.m[k] / 2);
       j->K[k] = 2 * j->h[k] + 1;
     }
-    const int64_t n0 = j->g.nf[0], n1 = j->g.nf[1], n2 = j->g.nf[2];
+    const int64_t n1 = j->g.nf[1], n2 = j->g.nf[2];
     e = cudaMalloc(&j->b1, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       std::vector<float2> t(j->g.nf[k]);
@@ -966,6 +996,41 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
                   "job_create (pruned transform): %s", cudaGetErrorString(e));
     }
     j->pruned = true;
+    // second lane when its scratch is small next to the free device memory
+    const char* lanes = getenv("MPSQ_LANES");
+    const size_t extra = (size_t)a.ngrid * j->g.n_fine * cs + 2 * sizeof(int) * (nkeys + 1) +
+                         (size_t)j->cap * (rsize(prec) + cs) +
+                         sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0];
+    size_t free_b = 0, total_b = 0;
+    if (!(lanes && strcmp(lanes, "1") == 0) && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+        extra * 4 < free_b) {
+      cudaError_t e2 = cudaStreamCreateWithFlags(&j->s2, cudaStreamNonBlocking);
+      if (e2 == cudaSuccess) e2 = cudaEventCreateWithFlags(&j->fork, cudaEventDisableTiming);
+      if (e2 == cudaSuccess) e2 = cudaEventCreateWithFlags(&j->join, cudaEventDisableTiming);
+      auto A2 = [&](void** ptr, size_t bytes) {
+        if (e2 == cudaSuccess) e2 = cudaMalloc(ptr, std::max<size_t>(bytes, 16));
+      };
+      A2(&j->fine2, (size_t)a.ngrid * j->g.n_fine * cs);
+      A2((void**)&j->counts2, sizeof(int) * (nkeys + 1));
+      A2((void**)&j->starts2, sizeof(int) * (nkeys + 1));
+      A2(&j->recs2, (size_t)j->cap * rsize(prec));
+      A2(&j->str2, (size_t)j->cap * cs);
+      A2((void**)&j->b1_2, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
+      if (e2 == cudaSuccess) {
+        j->lane2 = true;
+      } else {  // run with one lane
+        cudaGetLastError();
+        cudaFree(j->fine2);
+        cudaFree(j->counts2);
+        cudaFree(j->starts2);
+        cudaFree(j->recs2);
+        cudaFree(j->str2);
+        cudaFree(j->b1_2);
+        j->fine2 = j->recs2 = j->str2 = nullptr;
+        j->counts2 = j->starts2 = nullptr;
+        j->b1_2 = nullptr;
+      }
+    }
   } else {
     rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
     if (rc) {
@@ -979,6 +1044,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
 }
 
 extern "C" int mpsq_job_destroy(mpsq_job* j) {
+  if (j && j->s2) cudaStreamSynchronize(j->s2);
   if (j && j->s) cudaStreamSynchronize(j->s);
   job_free(j);
   return MPSQ_OK;
@@ -1015,7 +1081,7 @@ template <typename T>
 static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
   using C = typename Cplx<T>::type;
   using R = typename RecOf<T>::type;
-  cudaStream_t s = j->s;
+  cudaStream_t s = j->s;  // the stream of the current frame's lane
   const SpreadArgs& a = j->sa;
   const int64_t nkeys = (int64_t)a.ngrid * a.n_tiles;
   const int bt = 256;
@@ -1026,26 +1092,42 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     if (prof) MPSQ_CUDA_TRY(cudaEventRecord(j->ev[k], s));
     return MPSQ_OK;
   };
+  // two lanes: even frames of the call on the job's stream, odd ones on the second lane,
+  // which first waits for everything queued on the job's stream (uploads included); the
+  // job's stream waits for the second lane at the end
+  const bool two = j->lane2 && !prof && count > 1;
+  cudaStream_t const main_s = j->s;
+  if (two) {
+    MPSQ_CUDA_TRY(cudaEventRecord(j->fork, main_s));
+    MPSQ_CUDA_TRY(cudaStreamWaitEvent(j->s2, j->fork, 0));
+  }
   for (int32_t t = first; t < first + count; ++t) {
+    const bool odd = two && ((t - first) & 1);
+    s = odd ? j->s2 : main_s;
+    int* const counts = odd ? j->counts2 : j->counts;
+    int* const starts = odd ? j->starts2 : j->starts;
+    void* const recs = odd ? j->recs2 : j->recs;
+    void* const str = odd ? j->str2 : j->str;
+    void* const fine = odd ? j->fine2 : j->fine;
+    float2* const b1 = odd ? j->b1_2 : j->b1;
     const float4* frame = j->traj + (size_t)t * j->d.n_atoms_frame;
     if (mark(0)) return MPSQ_ERR_CUDA;
-    MPSQ_CUDA_TRY(cudaMemsetAsync(j->counts, 0, sizeof(int) * (nkeys + 1), s));
+    MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 0, j->counts, j->starts,
-                                          (R*)j->recs, (C*)j->str, j->cap, j->err);
+      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 0, counts, starts,
+                                          (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
-    int rc = launch_scan<T>(j->counts, j->starts, nkeys, s);
+    int rc = launch_scan<T>(counts, starts, nkeys, s);
     if (rc) return rc;
-    MPSQ_CUDA_TRY(cudaMemsetAsync(j->counts, 0, sizeof(int) * (nkeys + 1), s));
+    MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 1, j->counts, j->starts,
-                                          (R*)j->recs, (C*)j->str, j->cap, j->err);
+      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 1, counts, starts,
+                                          (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
     if (mark(1)) return MPSQ_ERR_CUDA;
-    rc = launch_spread<T>(a, (const R*)j->recs, (const C*)j->str, j->starts, j->pa.pack != 0,
-                          (C*)j->fine, s);
+    rc = launch_spread<T>(a, (const R*)recs, (const C*)str, starts, j->pa.pack != 0, (C*)fine, s);
     if (rc) return rc;
     if (mark(2)) return MPSQ_ERR_CUDA;
     C* csf = (C*)j->cs + (size_t)t * nm;
@@ -1054,10 +1136,10 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     if constexpr (sizeof(T) == 4) {
       if (j->pruned) {
         PruneLaunch pl;
-        pl.fine = (const float2*)j->fine;
+        pl.fine = (const float2*)fine;
         pl.n_fine = a.n_fine;
-        pl.b1 = j->b1;
-        pl.b2 = (float2*)j->fine;  // the fine grids are dead after pass X
+        pl.b1 = b1;
+        pl.b2 = (float2*)fine;  // the fine grids are dead after pass X
         for (int k = 0; k < 3; ++k) {
           pl.n[k] = (int)j->g.nf[k];
           pl.m[k] = (int)j->g.m[k];
@@ -1094,6 +1176,10 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
       }
       j->stage_frames += 1;
     }
+  }
+  if (two) {
+    MPSQ_CUDA_TRY(cudaEventRecord(j->join, j->s2));
+    MPSQ_CUDA_TRY(cudaStreamWaitEvent(main_s, j->join, 0));
   }
   return MPSQ_OK;
 }

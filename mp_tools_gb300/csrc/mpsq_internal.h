@@ -108,12 +108,16 @@ struct SpreadArgs {
   int ngrid;
   double gscale[3];  // nf / (2 pi): radians -> fine-grid units
   double ginv[3];    // 1 / nf
+  int tshift[3];     // log2(tile): tiles are powers of two
 };
 
 inline void finish_spread_args(SpreadArgs& a) {
   for (int k = 0; k < 3; ++k) {
     a.gscale[k] = (double)a.nf[k] * 0.15915494309189533576888376337251436;
     a.ginv[k] = 1.0 / (double)a.nf[k];
+    int sh = 0;
+    while ((1 << sh) < a.tile[k]) ++sh;
+    a.tshift[k] = sh;
   }
 }
 
@@ -212,11 +216,10 @@ __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3
     if (k < a.dim) {
       const int s = s_in[k];        // first cell of the support
       const int e = s + a.w - 1;    // last cell
-      const int t = a.tile[k];
       i0[k] = s;
       d[k] = d_in[k];
-      tlo[k] = s >= 0 ? s / t : -((t - 1 - s) / t);   // >= -1 since s >= -w and t >= w
-      thi[k] = e >= 0 ? e / t : -((t - 1 - e) / t);   // <= ntile since e < nf + t
+      tlo[k] = s >> a.tshift[k];    // floor division: >= -1 since s >= -w and tile >= w
+      thi[k] = e >> a.tshift[k];    // <= ntile since e < nf + tile
     } else {
       i0[k] = 0;
       d[k] = (T)0;
@@ -225,13 +228,13 @@ __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3
   }
   for (int tz = tlo[2]; tz <= thi[2]; ++tz) {
     const int wz = tz < 0 ? tz + a.ntile[2] : (tz >= a.ntile[2] ? tz - a.ntile[2] : tz);
-    const int lz = i0[2] - tz * a.tile[2];
+    const int lz = i0[2] - (tz << a.tshift[2]);
     for (int ty = tlo[1]; ty <= thi[1]; ++ty) {
       const int wy = ty < 0 ? ty + a.ntile[1] : (ty >= a.ntile[1] ? ty - a.ntile[1] : ty);
-      const int ly = i0[1] - ty * a.tile[1];
+      const int ly = i0[1] - (ty << a.tshift[1]);
       for (int tx = tlo[0]; tx <= thi[0]; ++tx) {
         const int wx = tx < 0 ? tx + a.ntile[0] : (tx >= a.ntile[0] ? tx - a.ntile[0] : tx);
-        const int lx = i0[0] - tx * a.tile[0];
+        const int lx = i0[0] - (tx << a.tshift[0]);
         const int64_t key = (int64_t)keygrid * a.n_tiles + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx;
         const int slot = atomicAdd(&cursor[key], 1);
         if (!scatter) continue;

@@ -150,3 +150,41 @@ def test_transform_from_host_equals_device_upload(cuda):
     finally:
         a.close()
         b.close()
+
+
+_CHILD_LANES = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests")
+import test_kernels_gpu as T
+from mp_tools_gb300 import _lib, sql
+fr, counts = T._alloy(n_atoms=4000, F=9)
+grid = sql.SqlGrid(4.0, (30.0,) * 3)
+job = T.SqomJob(grid, species_counts=counts, n_frames=fr.shape[0], precision=_lib.FP32, eps=1e-6,
+                n_atoms_frame=fr.shape[1], weight_mode=_lib.WEIGHT_XRAY, xff=[T.XFF_AL, T.XFF_U])
+job.set_frames(fr)
+job.transform(0, 4)            # even count
+job.transform(4, 5)            # odd count, second call
+job.sync()
+np.save(sys.argv[2], np.concatenate([job.amplitudes().ravel(), job.sq_total()]))
+job.close()
+"""
+XFF_AL = [6.4202, 3.0387, 1.9002, 0.7426, 1.5936, 31.5472, 1.9646, 85.0886, 1.1151]
+XFF_U = [36.0228, 0.5293, 23.4128, 3.3253, 14.9491, 16.0927, 4.1880, 100.6130, 13.3966]
+
+
+def test_two_frame_lanes_match_one_lane(cuda, tmp_path):
+    """Frames alternating between the job's stream and the second lane give the results of a
+    single lane (MPSQ_LANES=1, child process) to FP32 rounding, over two transform calls."""
+    out = {}
+    for lanes in ("2", "1"):
+        env = dict(os.environ)
+        if lanes == "1":
+            env["MPSQ_LANES"] = "1"
+        else:
+            env.pop("MPSQ_LANES", None)
+        path = tmp_path / f"lanes_{lanes}.npy"
+        subprocess.run([sys.executable, "-c", _CHILD_LANES, str(ROOT), str(path)], check=True,
+                       env=env, timeout=600)
+        out[lanes] = np.load(path)
+    assert rel_l2(out["2"], out["1"]) < 2e-6
