@@ -208,6 +208,26 @@ int mpsq_job_sqw_dispersion(mpsq_job* job, int32_t n_int, const float* t_wind,
                             int32_t n_path, const int64_t* q_index, int32_t n_freq,
                             const float* q2_norm, double scale, float* out, int host);
 
+/* Atom-pair forms of the two maps above (mp_sqom's j_atc1/j_atc2 option,
+ * code/src/mp_sqom56.f90:1460-1464 and :1494-1499): the series is the sum of the raw
+ * (unweighted, not mean-subtracted) amplitudes of species sp1 and sp2 (0-based), so the job
+ * must have been created with store_species = 1. */
+int mpsq_job_sqw_econst_pair(mpsq_job* job, int32_t n_int, const float* t_wind, int32_t j_freq,
+                             int32_t sp1, int32_t sp2, double scale, float* out, int host);
+int mpsq_job_sqw_dispersion_pair(mpsq_job* job, int32_t n_int, const float* t_wind,
+                                 int32_t n_path, const int64_t* q_index, int32_t n_freq,
+                                 int32_t sp1, int32_t sp2, double scale, float* out, int host);
+
+/* Intermediate scattering function I(Q,t) (mp_sqom's j_sq != 1 branch) on the mean-subtracted,
+ * optionally 1/|Q|-scaled amplitudes x:
+ *   map at lag `lag` (:1467-1472): out[q] = Re sum_{i<n_int} x(i+lag) conj(x(i)) / n_int * scale
+ *   along a path (:1504-1510):     out[p*n_lag + t] = Re sum_{i<n_int} x(t+i) conj(x(i)) * scale,
+ *                                  t < n_lag = n_frames - n_int + 1 (:699). */
+int mpsq_job_iqt(mpsq_job* job, int32_t n_int, int32_t lag, const float* q2_norm, double scale,
+                 float* out, int host);
+int mpsq_job_iqt_dispersion(mpsq_job* job, int32_t n_int, int32_t n_path, const int64_t* q_index,
+                            const float* q2_norm, double scale, float* out, int host);
+
 /* Gaussian-window spectrum over the whole run: for every Q, |sum_t g_t (cs - <cs>)
  * exp(-2pi i k t/n_frames)|^2 for k = 0..n_freq-1, g_t = exp(-4 ln2 (t-tc)^2/fwhm^2).
  * n_frames must be a power of two <= 1024.  out: n_freq x n_Q floats (Q fastest). */

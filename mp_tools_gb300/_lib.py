@@ -27,7 +27,9 @@ EXPORTS = [
     "mpsq_job_create", "mpsq_job_destroy", "mpsq_job_estimate_bytes", "mpsq_job_set_frames",
     "mpsq_job_set_frames_on",
     "mpsq_job_set_cell_index", "mpsq_job_transform", "mpsq_job_amplitudes", "mpsq_job_sq_total",
-    "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_gauss", "mpsq_job_sync",
+    "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_econst_pair",
+    "mpsq_job_sqw_dispersion_pair", "mpsq_job_iqt", "mpsq_job_iqt_dispersion",
+    "mpsq_job_sqw_gauss", "mpsq_job_sync",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
     "mpsq_version", "mpsq_launch_count",
     "mpsq_nufft2d1_noalloc",
@@ -116,6 +118,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_job_sqw_econst": (C.c_int, [vp, i32, vp, i32, vp, dbl, vp, C.c_int]),
         "mpsq_job_sqw_dispersion": (C.c_int, [vp, i32, vp, i32, vp, i32, vp, dbl, vp, C.c_int]),
         "mpsq_job_sqw_gauss": (C.c_int, [vp, dbl, i32, vp, dbl, vp, C.c_int]),
+        "mpsq_job_sqw_econst_pair": (C.c_int, [vp, i32, vp, i32, i32, i32, dbl, vp, C.c_int]),
+        "mpsq_job_sqw_dispersion_pair": (C.c_int, [vp, i32, vp, i32, vp, i32, i32, i32, dbl, vp, C.c_int]),
+        "mpsq_job_iqt": (C.c_int, [vp, i32, i32, vp, dbl, vp, C.c_int]),
+        "mpsq_job_iqt_dispersion": (C.c_int, [vp, i32, i32, vp, vp, dbl, vp, C.c_int]),
         "mpsq_job_sync": (C.c_int, [vp]),
         "mpsq_job_profile": (C.c_int, [vp, C.c_int]),
         "mpsq_job_stage_ms": (C.c_int, [vp, vp, vp, C.c_int]),

@@ -2,7 +2,9 @@
 //  * total S(Q) = sum_t |cs|^2 / nfile                      (mp_sqom56.f90:1381-1387)
 //  * E=const map, sliding Hann window, one frequency bin     (:1437-1478, window :941-948)
 //  * E(Q) dispersion cut, windowed DFT per start frame       (:1480-1517)
-//  * Gaussian-window spectrum over the whole run (one FFT per Q, radix-2 in shared memory)
+//  * Gaussian-window spectrum over the whole run (one FFT per Q in shared memory)
+//  * I(Q,t) maps and path cuts (the j_sq /= 1 branch, :1467-1472, :1504-1510)
+//  * atom-pair forms of the E=const map and E(Q) cut (raw sum of two species, :1460-1464)
 // The ω-resolved forms subtract the elastic mean <cs>_t first (:1177-1185, :1359-1376) and
 // optionally scale by 1/|Q| (:1373).  Sums over frames are compensated (FP32) or FP64.
 #include <cuda_runtime.h>
@@ -46,12 +48,24 @@ __global__ void sq_total_kernel(const typename Cplx<T>::type* __restrict__ cs, i
   out[q] = (float)(a.value() * scale);
 }
 
-// Loads a [nt x QT] tile of cs into shared memory, subtracts the column means and applies
-// the optional 1/|Q| factor.  Thread layout: column = tid % QT, part = tid / QT.
+// The time series a map is formed from: x(t, q) = a[t*stride + q] (+ b[t*stride + q]).  The
+// job's weighted amplitudes (a = cs, stride n_Q, centred: the elastic mean is subtracted) or
+// the raw sum of two stored species amplitudes (the atom-pair modes, not centred).
 template <typename T>
-__device__ void load_centered_tile(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
-                                   int nt, int64_t q0, int QT, const float* __restrict__ q2n,
-                                   typename Cplx<T>::type* xs, T* red_re, T* red_im) {
+struct Series {
+  const typename Cplx<T>::type* a;
+  const typename Cplx<T>::type* b;
+  int64_t stride;
+  int center;
+};
+
+// Loads a [nt x QT] tile of the series into shared memory, subtracts the column means (if
+// centred) and applies the optional 1/|Q| factor.  Thread layout: column = tid % QT,
+// part = tid / QT.
+template <typename T>
+__device__ void load_centered_tile(Series<T> src, int64_t nq, int nt, int64_t q0, int QT,
+                                   const float* __restrict__ q2n, typename Cplx<T>::type* xs,
+                                   T* red_re, T* red_im) {
   using C = typename Cplx<T>::type;
   const int tid = threadIdx.x, NT = blockDim.x;
   for (int e = tid; e < nt * QT; e += NT) {
@@ -60,10 +74,31 @@ __device__ void load_centered_tile(const typename Cplx<T>::type* __restrict__ cs
     C v;
     v.x = 0;
     v.y = 0;
-    if (q < nq) v = cs[(int64_t)t * nq + q];
+    if (q < nq) {
+      v = src.a[(int64_t)t * src.stride + q];
+      if (src.b) {
+        const C u = src.b[(int64_t)t * src.stride + q];
+        v.x += u.x;
+        v.y += u.y;
+      }
+    }
     xs[e] = v;
   }
   __syncthreads();
+  if (!src.center) {
+    if (q2n) {
+      for (int e = tid; e < nt * QT; e += NT) {
+        const int64_t q = q0 + e % QT;
+        const T f = q < nq ? (T)q2n[q] : (T)1;
+        C v = xs[e];
+        v.x *= f;
+        v.y *= f;
+        xs[e] = v;
+      }
+      __syncthreads();
+    }
+    return;
+  }
   const int col = tid % QT, part = tid / QT, nparts = NT / QT;
   T sr = 0, si = 0;
   if (part < nparts)
@@ -99,7 +134,7 @@ __device__ void load_centered_tile(const typename Cplx<T>::type* __restrict__ cs
 // E=const map: S(Q) = sum_{t0} | sum_i ph_i x(t0+i) |^2 with ph_i = t_wind_i exp(-2 pi i
 // (j_freq-1)(i - n_int/2)/n_int) (0-based i), times scale.
 template <typename T>
-__global__ void econst_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq, int nt,
+__global__ void econst_kernel(Series<T> cs, int64_t nq, int nt,
                               int QT, int n_int, const float* __restrict__ t_wind, int jf,
                               const float* __restrict__ q2n, double scale,
                               float* __restrict__ out) {
@@ -158,7 +193,7 @@ __global__ void econst_kernel(const typename Cplx<T>::type* __restrict__ cs, int
 
 // Dispersion: for path point p (one CTA), acc[f] = sum_{t0} |sum_i w_i x(t0+i) e^{-2 pi i f i/n}|^2.
 template <typename T>
-__global__ void dispersion_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+__global__ void dispersion_kernel(Series<T> cs, int64_t nq,
                                   int nt, const int64_t* __restrict__ qidx, int n_int,
                                   const float* __restrict__ t_wind, int n_freq,
                                   const float* __restrict__ q2n, double scale,
@@ -220,7 +255,7 @@ __global__ void dispersion_kernel(const typename Cplx<T>::type* __restrict__ cs,
 // Gaussian-window spectrum: per Q column, X_k = sum_t g_t (x_t - <x>) e^{-2 pi i k t/nt},
 // out[k][q] = |X_k|^2 * scale for k < n_freq.  nt = 2^p <= 1024, radix-2 in shared memory.
 template <typename T>
-__global__ void gauss_fft_kernel(const typename Cplx<T>::type* __restrict__ cs, int64_t nq,
+__global__ void gauss_fft_kernel(Series<T> cs, int64_t nq,
                                  int nt, int logn, int QT, const float* __restrict__ gwin,
                                  int n_freq, const float* __restrict__ q2n, double scale,
                                  float* __restrict__ out) {
@@ -300,6 +335,66 @@ __global__ void gauss_fft_kernel(const typename Cplx<T>::type* __restrict__ cs, 
     if (q >= nq) continue;
     const C v = xs[k * QT + c];
     out[(int64_t)k * nq + q] = (float)((double)(v.x * v.x + v.y * v.y) * scale);
+  }
+}
+
+// I(Q,t) map at lag `lag`: out[q] = Re sum_{i<n_int} x(i+lag) conj(x(i)) / n_int * scale.
+template <typename T>
+__global__ void iqt_kernel(Series<T> cs, int64_t nq, int nt, int QT, int n_int, int lag,
+                           const float* __restrict__ q2n, double scale, float* __restrict__ out) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int NT = blockDim.x, tid = threadIdx.x;
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  T* red_re = reinterpret_cast<T*>(xs + (size_t)nt * QT);
+  T* red_im = red_re + NT + QT;
+  const int64_t q0 = (int64_t)blockIdx.x * QT;
+  load_centered_tile<T>(cs, nq, nt, q0, QT, q2n, xs, red_re, red_im);
+  const int col = tid % QT, part = tid / QT, nparts = NT / QT;
+  Acc<T> acc;
+  if (part < nparts)
+    for (int i = part; i < n_int; i += nparts) {
+      const C a = xs[(i + lag) * QT + col], b = xs[i * QT + col];
+      acc.add(a.x * b.x + a.y * b.y);   // Re(a conj b)
+    }
+  __syncthreads();
+  red_re[tid] = (T)acc.value();
+  __syncthreads();
+  if (tid < QT) {
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p) s += (double)red_re[p * QT + tid];
+    const int64_t q = q0 + tid;
+    if (q < nq) out[q] = (float)(s / n_int * scale);
+  }
+}
+
+// I(Q,t) along a path: one CTA per path point, out[p * n_lag + t] = Re sum_{i<n_int}
+// x(t+i) conj(x(i)) * scale for t < n_lag = nt - n_int + 1.
+template <typename T>
+__global__ void iqt_dispersion_kernel(Series<T> cs, int64_t nq, int nt,
+                                      const int64_t* __restrict__ qidx, int n_int,
+                                      const float* __restrict__ q2n, double scale,
+                                      float* __restrict__ out) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int NT = blockDim.x, tid = threadIdx.x;
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  T* red_re = reinterpret_cast<T*>(xs + nt);
+  T* red_im = red_re + NT + 1;
+  const int n_lag = nt - n_int + 1;
+  const int64_t q = qidx[blockIdx.x];
+  if (q < 0 || q >= nq) {
+    for (int t = tid; t < n_lag; t += NT) out[(int64_t)blockIdx.x * n_lag + t] = 0.0f;
+    return;
+  }
+  load_centered_tile<T>(cs, nq, nt, q, 1, q2n, xs, red_re, red_im);
+  for (int t = tid; t < n_lag; t += NT) {
+    Acc<T> acc;
+    for (int i = 0; i < n_int; ++i) {
+      const C a = xs[t + i], b = xs[i];
+      acc.add(a.x * b.x + a.y * b.y);
+    }
+    out[(int64_t)blockIdx.x * n_lag + t] = (float)(acc.value() * scale);
   }
 }
 
@@ -482,10 +577,36 @@ extern "C" int mpsq_job_sq_total(mpsq_job* j, double norm2, float* out, int host
 }
 
 // q2_norm and t_wind are host arrays (n_Q and n_int floats).
-extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wind,
-                                   int32_t j_freq, const float* q2_norm, double scale,
-                                   float* out, int host) {
-  if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst: null pointer");
+namespace {
+// Source of a map: the weighted amplitudes (centred) or the raw sum of two stored species.
+struct SeriesArgs {
+  const void* a;
+  const void* b;
+  int64_t stride;
+  int center;
+};
+SeriesArgs weighted_series(const JobView& v) { return {v.cs, nullptr, v.n_q, 1}; }
+int pair_series(const JobView& v, int32_t sp1, int32_t sp2, const char* where, SeriesArgs* out) {
+  if (!v.store_species || !v.cs_species)
+    return fail(MPSQ_ERR_STATE, "%s: the atom-pair modes need a job created with store_species = 1", where);
+  if (sp1 < 0 || sp2 < 0 || sp1 >= v.n_species || sp2 >= v.n_species)
+    return fail(MPSQ_ERR_ARG, "%s: species %d, %d outside 0..%d", where, sp1, sp2, v.n_species - 1);
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const char* base = (const char*)v.cs_species;
+  out->a = base + (size_t)sp1 * v.n_q * csz;
+  out->b = base + (size_t)sp2 * v.n_q * csz;
+  out->stride = (int64_t)v.n_species * v.n_q;
+  out->center = 0;
+  return MPSQ_OK;
+}
+template <typename T>
+Series<T> typed(const SeriesArgs& s) {
+  using C = typename Cplx<T>::type;
+  return Series<T>{(const C*)s.a, (const C*)s.b, s.stride, s.center};
+}
+
+int econst_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const float* t_wind,
+                int32_t j_freq, const float* q2_norm, double scale, float* out, int host) {
   JobView v = job_view(j);
   if (n_int < 1 || n_int > v.n_frames)
     return fail(MPSQ_ERR_ARG, "sqw_econst: n_int %d outside 1..n_frames (%d)", n_int, v.n_frames);
@@ -510,11 +631,11 @@ extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wi
   const int jf = j_freq - 1;
   if (v.precision == MPSQ_FP64) {
     cudaFuncSetAttribute(econst_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    econst_kernel<double><<<nb, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, v.n_frames, QT, n_int,
+    econst_kernel<double><<<nb, NT, smem, v.s>>>(typed<double>(src), v.n_q, v.n_frames, QT, n_int,
                                                  dw, jf, dq, scale, b.dev);
   } else {
     cudaFuncSetAttribute(econst_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    econst_kernel<float><<<nb, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, v.n_frames, QT, n_int, dw,
+    econst_kernel<float><<<nb, NT, smem, v.s>>>(typed<float>(src), v.n_q, v.n_frames, QT, n_int, dw,
                                                 jf, dq, scale, b.dev);
   }
   count_launch();
@@ -527,11 +648,9 @@ extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wi
   return rc;
 }
 
-extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* t_wind,
-                                       int32_t n_path, const int64_t* q_index, int32_t n_freq,
-                                       const float* q2_norm, double scale, float* out,
-                                       int host) {
-  if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion: null pointer");
+int dispersion_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const float* t_wind,
+                    int32_t n_path, const int64_t* q_index, int32_t n_freq,
+                    const float* q2_norm, double scale, float* out, int host) {
   JobView v = job_view(j);
   if (n_int < 1 || n_int > v.n_frames) return fail(MPSQ_ERR_ARG, "sqw_dispersion: bad n_int");
   if (n_path < 1 || n_freq < 1 || n_freq > n_int) return fail(MPSQ_ERR_ARG, "sqw_dispersion: bad sizes");
@@ -554,11 +673,11 @@ extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* 
   }
   if (v.precision == MPSQ_FP64) {
     cudaFuncSetAttribute(dispersion_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    dispersion_kernel<double><<<n_path, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, v.n_frames, di,
+    dispersion_kernel<double><<<n_path, NT, smem, v.s>>>(typed<double>(src), v.n_q, v.n_frames, di,
                                                          n_int, dw, n_freq, dq, scale, b.dev);
   } else {
     cudaFuncSetAttribute(dispersion_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    dispersion_kernel<float><<<n_path, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, v.n_frames, di,
+    dispersion_kernel<float><<<n_path, NT, smem, v.s>>>(typed<float>(src), v.n_q, v.n_frames, di,
                                                         n_int, dw, n_freq, dq, scale, b.dev);
   }
   count_launch();
@@ -567,6 +686,129 @@ extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* 
                         : fail(MPSQ_ERR_CUDA, "dispersion launch: %s", cudaGetErrorString(e));
   cudaStreamSynchronize(v.s);
   cudaFree(dw);
+  cudaFree(dq);
+  cudaFree(di);
+  return rc;
+}
+}  // namespace
+
+extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                   int32_t j_freq, const float* q2_norm, double scale,
+                                   float* out, int host) {
+  if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst: null pointer");
+  return econst_impl(j, weighted_series(job_view(j)), n_int, t_wind, j_freq, q2_norm, scale, out,
+                     host);
+}
+
+extern "C" int mpsq_job_sqw_econst_pair(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                        int32_t j_freq, int32_t sp1, int32_t sp2, double scale,
+                                        float* out, int host) {
+  if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst_pair: null pointer");
+  SeriesArgs src;
+  const int rc = pair_series(job_view(j), sp1, sp2, "sqw_econst_pair", &src);
+  if (rc) return rc;
+  return econst_impl(j, src, n_int, t_wind, j_freq, nullptr, scale, out, host);
+}
+
+extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                       int32_t n_path, const int64_t* q_index, int32_t n_freq,
+                                       const float* q2_norm, double scale, float* out,
+                                       int host) {
+  if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion: null pointer");
+  return dispersion_impl(j, weighted_series(job_view(j)), n_int, t_wind, n_path, q_index, n_freq,
+                         q2_norm, scale, out, host);
+}
+
+extern "C" int mpsq_job_sqw_dispersion_pair(mpsq_job* j, int32_t n_int, const float* t_wind,
+                                            int32_t n_path, const int64_t* q_index,
+                                            int32_t n_freq, int32_t sp1, int32_t sp2,
+                                            double scale, float* out, int host) {
+  if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion_pair: null pointer");
+  SeriesArgs src;
+  const int rc = pair_series(job_view(j), sp1, sp2, "sqw_dispersion_pair", &src);
+  if (rc) return rc;
+  return dispersion_impl(j, src, n_int, t_wind, n_path, q_index, n_freq, nullptr, scale, out,
+                         host);
+}
+
+extern "C" int mpsq_job_iqt(mpsq_job* j, int32_t n_int, int32_t lag, const float* q2_norm,
+                            double scale, float* out, int host) {
+  if (!j) return fail(MPSQ_ERR_ARG, "iqt: null job");
+  JobView v = job_view(j);
+  if (n_int < 1 || lag < 0 || lag + n_int > v.n_frames)
+    return fail(MPSQ_ERR_ARG, "iqt: lag %d + n_int %d exceeds n_frames %d", lag, n_int, v.n_frames);
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const int NT = 256;
+  const size_t extra = (size_t)2 * (NT + 32) * (csz / 2);
+  const int QT = tile_cols(v.n_frames, csz, extra, 200 * 1024);
+  if (QT == 0) return fail(MPSQ_ERR_ARG, "iqt: %d frames do not fit in shared memory", v.n_frames);
+  const size_t smem = (size_t)v.n_frames * QT * csz + (size_t)2 * (NT + QT) * (csz / 2);
+  float* dq = nullptr;
+  int rc = dev_copy(q2_norm, q2_norm ? v.n_q : 0, &dq, v.s);
+  OutBuf b;
+  if (!rc) rc = out_prepare(out, host, v.n_q, &b);
+  if (rc) {
+    cudaFree(dq);
+    return rc;
+  }
+  const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
+  const SeriesArgs src = weighted_series(v);
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(iqt_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    iqt_kernel<double><<<nb, NT, smem, v.s>>>(typed<double>(src), v.n_q, v.n_frames, QT, n_int, lag,
+                                              dq, scale, b.dev);
+  } else {
+    cudaFuncSetAttribute(iqt_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    iqt_kernel<float><<<nb, NT, smem, v.s>>>(typed<float>(src), v.n_q, v.n_frames, QT, n_int, lag,
+                                             dq, scale, b.dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  rc = e == cudaSuccess ? out_finish(out, host, v.n_q, &b, v.s)
+                        : fail(MPSQ_ERR_CUDA, "iqt launch: %s", cudaGetErrorString(e));
+  cudaStreamSynchronize(v.s);
+  cudaFree(dq);
+  return rc;
+}
+
+extern "C" int mpsq_job_iqt_dispersion(mpsq_job* j, int32_t n_int, int32_t n_path,
+                                       const int64_t* q_index, const float* q2_norm,
+                                       double scale, float* out, int host) {
+  if (!j || !q_index) return fail(MPSQ_ERR_ARG, "iqt_dispersion: null pointer");
+  JobView v = job_view(j);
+  if (n_int < 1 || n_int > v.n_frames || n_path < 1)
+    return fail(MPSQ_ERR_ARG, "iqt_dispersion: bad sizes");
+  const int n_lag = v.n_frames - n_int + 1;
+  const size_t csz = v.precision == MPSQ_FP64 ? 16 : 8;
+  const int NT = 128;
+  const size_t smem = (size_t)v.n_frames * csz + (size_t)2 * (NT + 2) * (csz / 2);
+  if (smem > 200 * 1024) return fail(MPSQ_ERR_ARG, "iqt_dispersion: too many frames");
+  float* dq = nullptr;
+  int64_t* di = nullptr;
+  int rc = dev_copy(q2_norm, q2_norm ? v.n_q : 0, &dq, v.s);
+  if (!rc) rc = dev_copy(q_index, n_path, &di, v.s);
+  OutBuf b;
+  if (!rc) rc = out_prepare(out, host, (size_t)n_path * n_lag, &b);
+  if (rc) {
+    cudaFree(dq);
+    cudaFree(di);
+    return rc;
+  }
+  const SeriesArgs src = weighted_series(v);
+  if (v.precision == MPSQ_FP64) {
+    cudaFuncSetAttribute(iqt_dispersion_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    iqt_dispersion_kernel<double><<<n_path, NT, smem, v.s>>>(typed<double>(src), v.n_q, v.n_frames,
+                                                             di, n_int, dq, scale, b.dev);
+  } else {
+    cudaFuncSetAttribute(iqt_dispersion_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    iqt_dispersion_kernel<float><<<n_path, NT, smem, v.s>>>(typed<float>(src), v.n_q, v.n_frames,
+                                                            di, n_int, dq, scale, b.dev);
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_path * n_lag, &b, v.s)
+                        : fail(MPSQ_ERR_CUDA, "iqt_dispersion launch: %s", cudaGetErrorString(e));
+  cudaStreamSynchronize(v.s);
   cudaFree(dq);
   cudaFree(di);
   return rc;
@@ -608,7 +850,7 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
   const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
   if (v.precision == MPSQ_FP64) {
     cudaFuncSetAttribute(gauss_fft_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    gauss_fft_kernel<double><<<nb, NT, smem, v.s>>>((const double2*)v.cs, v.n_q, nt, logn, QT, dg,
+    gauss_fft_kernel<double><<<nb, NT, smem, v.s>>>(typed<double>(weighted_series(v)), v.n_q, nt, logn, QT, dg,
                                                     n_freq, dq, scale, b.dev);
   } else if (nt >= 64) {
     const float2* cs = (const float2*)v.cs;
@@ -622,7 +864,7 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
     }
   } else {
     cudaFuncSetAttribute(gauss_fft_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    gauss_fft_kernel<float><<<nb, NT, smem, v.s>>>((const float2*)v.cs, v.n_q, nt, logn, QT, dg,
+    gauss_fft_kernel<float><<<nb, NT, smem, v.s>>>(typed<float>(weighted_series(v)), v.n_q, nt, logn, QT, dg,
                                                    n_freq, dq, scale, b.dev);
   }
   count_launch();

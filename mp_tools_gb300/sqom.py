@@ -410,22 +410,31 @@ class SqomJob:
         return res
 
     def sqw_econst(self, taxis: TimeAxis, j_freq: int, q2_norm=None, normalize=True,
-                   t_wind=None) -> np.ndarray:
-        """E=const map for 1-based bin j_freq (:1437-1478), normalised as :1527, :1575-1576."""
+                   t_wind=None, atom_pair=None) -> np.ndarray:
+        """E=const map for 1-based bin j_freq (:1437-1478), normalised as :1527, :1575-1576.
+        atom_pair=(a, b): the map of the raw amplitudes of species a + b (0-based; :1460-1464;
+        needs store_species), where q2_norm does not apply."""
         w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
         scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
         if normalize:
             scale *= taxis.t_step / self.norm2()
         res = np.empty(self.grid.n_modes, f32)
-        check(_lib.load().mpsq_job_sqw_econst(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
-                                              C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
-              "sqw_econst")
+        L = _lib.load()
+        if atom_pair is None:
+            check(L.mpsq_job_sqw_econst(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
+                                        C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
+                  "sqw_econst")
+        else:
+            check(L.mpsq_job_sqw_econst_pair(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
+                                             int(atom_pair[0]), int(atom_pair[1]), scale,
+                                             C.c_void_p(ptr(res)), 1), "sqw_econst_pair")
         return res
 
     def sqw_dispersion(self, taxis: TimeAxis, q_index, n_freq=None, q2_norm=None,
-                       normalize=True, t_wind=None) -> np.ndarray:
-        """E(Q) cut along pixel indices q_index (:1480-1517); returns (n_path, n_freq)."""
+                       normalize=True, t_wind=None, atom_pair=None) -> np.ndarray:
+        """E(Q) cut along pixel indices q_index (:1480-1517); returns (n_path, n_freq).
+        atom_pair=(a, b): the cut of the raw amplitudes of species a + b (:1494-1499)."""
         w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
         qi = np.ascontiguousarray(q_index, np.int64)
         n_freq = taxis.n_freq_max if n_freq is None else n_freq
@@ -434,9 +443,38 @@ class SqomJob:
         if normalize:
             scale *= taxis.t_step / self.norm2()
         res = np.empty((len(qi), n_freq), f32)
-        check(_lib.load().mpsq_job_sqw_dispersion(self._h, taxis.n_int, C.c_void_p(ptr(w)), len(qi),
-                                                  C.c_void_p(ptr(qi)), n_freq, C.c_void_p(ptr(q2)),
-                                                  scale, C.c_void_p(ptr(res)), 1), "sqw_dispersion")
+        L = _lib.load()
+        if atom_pair is None:
+            check(L.mpsq_job_sqw_dispersion(self._h, taxis.n_int, C.c_void_p(ptr(w)), len(qi),
+                                            C.c_void_p(ptr(qi)), n_freq, C.c_void_p(ptr(q2)),
+                                            scale, C.c_void_p(ptr(res)), 1), "sqw_dispersion")
+        else:
+            check(L.mpsq_job_sqw_dispersion_pair(self._h, taxis.n_int, C.c_void_p(ptr(w)), len(qi),
+                                                 C.c_void_p(ptr(qi)), n_freq, int(atom_pair[0]),
+                                                 int(atom_pair[1]), scale, C.c_void_p(ptr(res)), 1),
+                  "sqw_dispersion_pair")
+        return res
+
+    def iqt(self, n_int: int, lag: int, q2_norm=None, normalize=True) -> np.ndarray:
+        """I(Q,t) map at a time lag of `lag` frames (the j_sq /= 1 branch, :1467-1472),
+        normalised by (sum N)^2 (:1573-1574)."""
+        q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
+        scale = 1.0 / self.norm2() if normalize else 1.0
+        res = np.empty(self.grid.n_modes, f32)
+        check(_lib.load().mpsq_job_iqt(self._h, int(n_int), int(lag), C.c_void_p(ptr(q2)), scale,
+                                       C.c_void_p(ptr(res)), 1), "iqt")
+        return res
+
+    def iqt_dispersion(self, n_int: int, q_index, q2_norm=None, normalize=True) -> np.ndarray:
+        """I(Q,t) along pixel indices q_index for lags 0..n_frames-n_int (:1504-1510, :699);
+        returns (n_path, n_frames - n_int + 1)."""
+        qi = np.ascontiguousarray(q_index, np.int64)
+        q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
+        scale = 1.0 / self.norm2() if normalize else 1.0
+        res = np.empty((len(qi), self.n_frames - int(n_int) + 1), f32)
+        check(_lib.load().mpsq_job_iqt_dispersion(self._h, int(n_int), len(qi), C.c_void_p(ptr(qi)),
+                                                  C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
+              "iqt_dispersion")
         return res
 
     def sqw_gauss(self, fwhm_frames=None, n_freq=None, t_step=1.0, q2_norm=None, normalize=True,

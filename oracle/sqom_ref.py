@@ -117,10 +117,12 @@ def hann_window(n_int, variant="symmetric"):
     return 0.5 * (1.0 - np.cos(2 * np.pi * i / (n_int + 1)))
 
 
-def econst(cs, n_int, t_wind, j_freq, q2_norm=None, scale=1.0):
+def econst(cs, n_int, t_wind, j_freq, q2_norm=None, scale=1.0, center=True):
     """E=const map for 1-based bin j_freq (:1437-1478): sum over start frames of
-    |sum_i om_phase_i x(t0+i)|^2, om_phase_i = t_wind_i exp(-2 pi i (j_freq-1)(i-n_int/2-1)/n_int)."""
-    x = centered(cs, q2_norm)
+    |sum_i om_phase_i x(t0+i)|^2, om_phase_i = t_wind_i exp(-2 pi i (j_freq-1)(i-n_int/2-1)/n_int).
+    center=False takes cs as is: the atom-pair form (:1460-1464), where cs is the sum of two
+    species' raw amplitudes."""
+    x = centered(cs, q2_norm) if center else np.asarray(cs)
     F = x.shape[0]
     i = np.arange(1, n_int + 1)
     ph = np.asarray(t_wind) * np.exp(-2j * np.pi * (j_freq - 1) * (i - n_int // 2 - 1) / n_int)
@@ -132,10 +134,11 @@ def econst(cs, n_int, t_wind, j_freq, q2_norm=None, scale=1.0):
     return out * scale
 
 
-def dispersion(cs, n_int, t_wind, q_index, n_freq, q2_norm=None, scale=1.0):
+def dispersion(cs, n_int, t_wind, q_index, n_freq, q2_norm=None, scale=1.0, center=True):
     """E(Q) cut (:1480-1517): for each path index, sum over start frames of
-    |FFT(t_wind * x(t0 : t0+n_int))[0:n_freq]|^2 (forward, unscaled).  Returns (n_path, n_freq)."""
-    x = centered(cs, q2_norm)[:, np.asarray(q_index)]
+    |FFT(t_wind * x(t0 : t0+n_int))[0:n_freq]|^2 (forward, unscaled).  Returns (n_path, n_freq).
+    center=False: the atom-pair form (:1494-1499) on the raw sum of two species."""
+    x = (centered(cs, q2_norm) if center else np.asarray(cs))[:, np.asarray(q_index)]
     F = x.shape[0]
     n0 = F - n_int + 1
     out = np.zeros((x.shape[1], n_freq))
@@ -143,6 +146,26 @@ def dispersion(cs, n_int, t_wind, q_index, n_freq, q2_norm=None, scale=1.0):
     for t0 in range(n0):
         X = np.fft.fft(w * x[t0:t0 + n_int], axis=0)[:n_freq]
         out += (np.abs(X) ** 2).T
+    return out * scale
+
+
+def iqt_map(cs, n_int, lag, q2_norm=None, scale=1.0):
+    """I(Q,t) map at time lag `lag` (frames), the j_sq /= 1 branch of :1467-1472: the real
+    part of sum_{i<n_int} x(i+lag) conj(x(i)) / n_int, x = centred (1/|Q|-scaled) amplitudes."""
+    x = centered(cs, q2_norm)
+    v = (x[lag:lag + n_int] * np.conj(x[:n_int])).sum(axis=0) / n_int
+    return v.real * scale
+
+
+def iqt_dispersion(cs, n_int, q_index, q2_norm=None, scale=1.0):
+    """I(Q,t) along a path (:1504-1510, n_freq_max = nfile - n_int + 1 at :699): out[p, t] =
+    Re sum_{i<n_int} x(t+i, q_p) conj(x(i, q_p)) for t = 0..nfile-n_int."""
+    x = centered(cs, q2_norm)[:, np.asarray(q_index)]
+    F = x.shape[0]
+    n_lag = F - n_int + 1
+    out = np.zeros((x.shape[1], n_lag))
+    for t in range(n_lag):
+        out[:, t] = (x[t:t + n_int] * np.conj(x[:n_int])).sum(axis=0).real
     return out * scale
 
 

@@ -182,3 +182,52 @@ def test_pruned_transform_odd_and_mixed_mode_counts(cuda, n_q):
     job = run_job(grid, frames, counts, precision=_lib.FP32, eps=1e-6)
     ref = oracle_cs(frames, counts, grid)
     assert rel_l2(job.amplitudes(), ref) < 3e-5
+
+
+@pytest.mark.parametrize("prec,eps,tol", [(_lib.FP64, 1e-10, 1e-8), (_lib.FP32, 1e-6, 3e-5)])
+def test_intermediate_scattering_function(cuda, prec, eps, tol):
+    """I(Q,t) map and path cut (mp_sqom's j_sq /= 1 branch) vs the oracle on the job's own
+    amplitudes, with and without the 1/|Q| factor."""
+    frames, _, counts = cell_system(F=12, seed=4)
+    grid = QGrid(_lib.CELL, (4, 4, 4), n_bz=2, a_par=(4.19,) * 3, ndim=3)
+    job = run_job(grid, frames, counts, precision=prec, eps=eps, weight_mode=2,
+                  b_coh=[0.507, 0.716, 0.5803, 0.5803, 0.5803])
+    cs = job.amplitudes().astype(np.complex128)
+    q2 = grid.q2_norm()
+    n_int = 6
+    for lag in (0, 3, 6):
+        for qn in (None, q2):
+            got = job.iqt(n_int, lag, q2_norm=qn, normalize=False)
+            want = sqom_ref.iqt_map(cs, n_int, lag, qn)
+            assert rel_l2(got, want) < 1e-5
+    path = np.arange(0, grid.n_modes, 29)
+    got = job.iqt_dispersion(n_int, path, q2_norm=q2, normalize=False)
+    want = sqom_ref.iqt_dispersion(cs, n_int, path, q2)
+    assert got.shape == (len(path), 12 - n_int + 1)
+    assert rel_l2(got, want) < 1e-5
+    job.close()
+
+
+@pytest.mark.parametrize("prec,eps,tol", [(_lib.FP64, 1e-10, 1e-8), (_lib.FP32, 1e-6, 3e-5)])
+def test_atom_pair_maps(cuda, prec, eps, tol):
+    """E=const map and E(Q) cut of species pair (B, O1) (mp_sqom's j_atc1/j_atc2 option) vs the
+    oracle: raw amplitudes of the two species summed, no mean subtraction."""
+    frames, _, counts = cell_system(F=8, seed=5)
+    grid = QGrid(_lib.CELL, (4, 4, 4), n_bz=2, a_par=(4.19,) * 3, ndim=3)
+    job = run_job(grid, frames, counts, precision=prec, eps=eps, weight_mode=2,
+                  b_coh=[0.507, 0.716, 0.5803, 0.5803, 0.5803], store_species=True)
+    pair_sum = oracle_cs(frames, counts, grid, weight_mode=1, mask=[0, 1, 1, 0, 0])
+    ta = TimeAxis(nfile=8, t_step=0.01)
+    scale = 1.0 / (0.5 * ta.n_frame * ta.n_int)
+    for jf in (1, 2):
+        got = job.sqw_econst(ta, jf, normalize=False, atom_pair=(1, 2))
+        want = sqom_ref.econst(pair_sum, ta.n_int, ta.window(), jf, None, scale, center=False)
+        assert rel_l2(got, want) < 1e-5        # maps are written as float32
+    path = np.arange(0, grid.n_modes, 31)
+    got = job.sqw_dispersion(ta, path, normalize=False, atom_pair=(1, 2))
+    want = sqom_ref.dispersion(pair_sum, ta.n_int, ta.window(), path, ta.n_freq_max, None, scale,
+                               center=False)
+    assert rel_l2(got, want) < 1e-5
+    with pytest.raises(_lib.MpsqError):
+        job.sqw_econst(ta, 1, atom_pair=(1, 7))
+    job.close()

@@ -117,3 +117,23 @@ def test_single_exponential_peaks_at_its_bin():
     cs2 = np.exp(+2j * np.pi * 5 * t / F)[:, None] * np.ones((1, 3))
     s2 = sqom_ref.gauss_spectrum(cs2, F / 2, F)
     assert np.all(np.argmax(s2, axis=0) == 5)
+
+
+def test_iqt_identities():
+    """I(Q,t) at lag 0 over the whole run is the mean-subtracted power; the path cut at lag t
+    equals n_int times the map at lag t on the path's pixels; atom-pair maps of a centred
+    series equal the weighted-series maps."""
+    rng = np.random.default_rng(11)
+    F, nq = 16, 40
+    cs = rng.normal(size=(F, nq)) + 1j * rng.normal(size=(F, nq))
+    x = sqom_ref.centered(cs)
+    np.testing.assert_allclose(sqom_ref.iqt_map(cs, F, 0), (np.abs(x) ** 2).mean(axis=0), rtol=1e-12)
+    path = np.array([3, 7, 30])
+    cut = sqom_ref.iqt_dispersion(cs, 6, path)
+    assert cut.shape == (3, F - 6 + 1)
+    for lag in (0, 4, 10):
+        np.testing.assert_allclose(cut[:, lag], 6 * sqom_ref.iqt_map(cs, 6, lag)[path], rtol=1e-12)
+    w = sqom_ref.hann_window(5)
+    a = sqom_ref.econst(cs, 5, w, 2)
+    b = sqom_ref.econst(x, 5, w, 2, center=False)
+    np.testing.assert_allclose(a, b, rtol=1e-12)
