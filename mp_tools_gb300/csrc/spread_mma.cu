@@ -30,6 +30,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -60,8 +62,62 @@ struct MmaSmem {
   int n0, b1, n1;
 };
 
-__device__ __forceinline__ float es_value(float z, float beta) {
-  return expf(beta * (sqrtf(fmaxf(1.0f - z * z, 0.0f)) - 1.0f));
+// The ES kernel value of cell i of a support, phi(z) = exp(beta (sqrt(1 - z^2) - 1)) at
+// z = (2 (u + i) - W) / W, u in [0, 1) the point's offset inside its first cell, as a
+// polynomial of degree W + 2 in v = 2u - 1 per cell (Chebyshev interpolation on the host,
+// monomial coefficients, Horner on the FMA pipe; no exp/sqrt on the special-function unit).
+// The interpolation error is below the kernel's own edge value e^-beta (about eps / 10).
+template <int W>
+struct EsPoly {
+  static constexpr int kDeg = W + 2;
+  float c[W][kDeg + 1];   // c[i][k]: coefficient of v^k for cell i
+};
+
+template <int W>
+__device__ __forceinline__ float es_cell(const EsPoly<W>& p, int i, float v) {
+  float r = p.c[i][EsPoly<W>::kDeg];
+#pragma unroll
+  for (int k = EsPoly<W>::kDeg - 1; k >= 0; --k) r = fmaf(r, v, p.c[i][k]);
+  return r;
+}
+
+// Chebyshev interpolation of phi on each cell, converted to monomials in v (FP64 on the host).
+template <int W>
+EsPoly<W> make_es_poly(double beta) {
+  constexpr int P = EsPoly<W>::kDeg;
+  EsPoly<W> out{};
+  for (int i = 0; i < W; ++i) {
+    double f[P + 1], a[P + 1];
+    for (int j = 0; j <= P; ++j) {
+      const double v = std::cos(M_PI * (j + 0.5) / (P + 1));
+      const double z = (2.0 * ((v + 1.0) * 0.5 + i) - W) / W;
+      f[j] = std::exp(beta * (std::sqrt(std::max(1.0 - z * z, 0.0)) - 1.0));
+    }
+    for (int k = 0; k <= P; ++k) {
+      double s = 0.0;
+      for (int j = 0; j <= P; ++j) s += f[j] * std::cos(M_PI * k * (j + 0.5) / (P + 1));
+      a[k] = 2.0 * s / (P + 1);
+    }
+    a[0] *= 0.5;
+    // sum_k a_k T_k(v) in monomials: T_0 = 1, T_1 = v, T_{k+1} = 2 v T_k - T_{k-1}
+    double t0[P + 1] = {}, t1[P + 1] = {}, m[P + 1] = {};
+    t0[0] = 1.0;
+    t1[1] = 1.0;
+    for (int q = 0; q <= P; ++q) m[q] += a[0] * t0[q];
+    if (P >= 1)
+      for (int q = 0; q <= P; ++q) m[q] += a[1] * t1[q];
+    for (int k = 2; k <= P; ++k) {
+      double tk[P + 1] = {};
+      for (int q = 0; q <= P; ++q) tk[q] = (q > 0 ? 2.0 * t1[q - 1] : 0.0) - t0[q];
+      for (int q = 0; q <= P; ++q) m[q] += a[k] * tk[q];
+      for (int q = 0; q <= P; ++q) {
+        t0[q] = t1[q];
+        t1[q] = tk[q];
+      }
+    }
+    for (int q = 0; q <= P; ++q) out.c[i][q] = (float)m[q];
+  }
+  return out;
 }
 
 __device__ __forceinline__ float clear_low13(float v) {
@@ -165,7 +221,7 @@ __global__ void __launch_bounds__(256, 3)
     spread3_pair_mma_kernel(SpreadArgs a, const RecF* __restrict__ recs,
                             const int* __restrict__ idx, const float2* __restrict__ cv,
                             int64_t c_stride, const int* __restrict__ starts,
-                            float2* __restrict__ fine) {
+                            float2* __restrict__ fine, const EsPoly<W> poly) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MmaSmem<W>& sm = *reinterpret_cast<MmaSmem<W>*>(smem_raw);
   constexpr int K1 = MmaSmem<W>::kKeys;
@@ -186,8 +242,6 @@ __global__ void __launch_bounds__(256, 3)
     for (int j = 0; j < 2; ++j)
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc_re[i][j][k] = acc_im[i][j][k] = 0.0f;
-  const float beta = (float)a.beta;
-  const float s2w = 2.0f / (float)W;
   const int r0 = starts[key], r1 = starts[key + 1];
   for (int c0 = r0; c0 < r1; c0 += kCap) {
     const int n = min(kCap, r1 - c0);
@@ -257,19 +311,23 @@ __global__ void __launch_bounds__(256, 3)
         const int lx = (q.packed & 0xff) - 64;
         const int ly = ((q.packed >> 8) & 0xff) - 64;
         const int lz = ((q.packed >> 16) & 0xff) - 64;
+        // offsets d in [-W/2, -W/2 + 1) -> polynomial variable v = 2d + W - 1 in [-1, 1)
+        const float vx = fmaf(2.0f, q.dx, (float)(W - 1));
+        const float vy = fmaf(2.0f, q.dy, (float)(W - 1));
+        const float vz = fmaf(2.0f, q.dz, (float)(W - 1));
         __half* xh = reinterpret_cast<__half*>(&sm.kxh[0][0]);
         __half* xl = reinterpret_cast<__half*>(&sm.kxl[0][0]);
 #pragma unroll
         for (int i = 0; i < W; ++i) {
           const int x = lx + i, y = ly + i, z = lz + i;
           if (x >= 0 && x < 16) {
-            const float v = es_value((q.dx + (float)i) * s2w, beta) * 1024.0f;
+            const float v = es_cell(poly, i, vx) * 1024.0f;
             const float h = clear_low13(v);
             xh[x * 2 * kKh + st] = __float2half_rn(h);
             xl[x * 2 * kKh + st] = __float2half_rn(v - h);
           }
-          if (y >= 0 && y < 16) sm.ky[y][st] = es_value((q.dy + (float)i) * s2w, beta) * s;
-          if (z >= 0 && z < 16) sm.kz[z][st] = es_value((q.dz + (float)i) * s2w, beta);
+          if (y >= 0 && y < 16) sm.ky[y][st] = es_cell(poly, i, vy) * s;
+          if (z >= 0 && z < 16) sm.kz[z][st] = es_cell(poly, i, vz);
         }
         sm.lz[st] = lz;
       }
@@ -312,8 +370,20 @@ int launch_w(const SpreadArgs& a, const RecF* recs, const int* idx, const float2
                                 (int)sizeof(MmaSmem<W>));
   });
   if (attr != cudaSuccess) return fail(MPSQ_ERR_CUDA, "spread mma attribute: %s", cudaGetErrorString(attr));
+  static std::mutex mu;
+  static double cached_beta = -1.0;
+  static EsPoly<W> poly;
+  EsPoly<W> p;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (cached_beta != a.beta) {
+      poly = make_es_poly<W>(a.beta);
+      cached_beta = a.beta;
+    }
+    p = poly;
+  }
   spread3_pair_mma_kernel<W><<<dim3((unsigned)nkeys, (unsigned)ntrans), 256, sizeof(MmaSmem<W>), s>>>(
-      a, recs, idx, cv, c_stride, starts, fine);
+      a, recs, idx, cv, c_stride, starts, fine, p);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
