@@ -150,10 +150,11 @@ struct mpsq_job {
 namespace mpsq {
 
 // Selection, phases and strengths of one atom of one frame (mp_sqom56.f90:1104-1142), then
-// binning.  Pass 0 counts, pass 1 scatters.
-template <typename T>
+// binning.  Pass 0 (kScatter false) counts, pass 1 scatters; str == nullptr: unit strengths
+// (no centre phase, no window), which are not stored.
+template <typename T, bool kScatter>
 __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
-                               PrepArgs p, SpreadArgs a, int scatter, int* cursor,
+                               PrepArgs p, SpreadArgs a, int* cursor,
                                const int* __restrict__ starts, typename RecOf<T>::type* recs,
                                typename Cplx<T>::type* str, int64_t cap, int* err) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -185,9 +186,12 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
       const float rf[3] = {r.x, r.y, r.z};
       int sc[3] = {0, 0, 0};
       float dc[3] = {0.0f, 0.0f, 0.0f};
-      for (int k = 0; k < p.dim; ++k) {
-        const F2 gk = affine_f2(rf, p.ahi[k], p.alo[k], p.bhi[k], p.blo[k]);
-        split_cell_f2(gk, p.nf[k], p.inv_nf[k], a.w, &sc[k], &dc[k]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {  // unrolled: sc, dc stay in registers
+        if (k < p.dim) {
+          const F2 gk = affine_f2(rf, p.ahi[k], p.alo[k], p.bhi[k], p.blo[k]);
+          split_cell_f2(gk, p.nf[k], p.inv_nf[k], a.w, &sc[k], &dc[k]);
+        }
       }
       float2 c = make_float2(1.0f, 0.0f);
       if (p.has_qc) {
@@ -211,7 +215,7 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
       }
       const int comp = p.pack ? p.comp_of[s] : 0;
       if (p.pack && c.x == 0.0f) return;
-      emit_cells<float>(a, sc, dc, grid, comp, scatter != 0, cursor, starts, (RecF*)recs,
+      emit_cells<float>(a, sc, dc, grid, comp, kScatter, cursor, starts, (RecF*)recs,
                         (float2*)str, c, nullptr, 0, cap, err);
       return;
     }
@@ -280,7 +284,7 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
   }
   const int comp = p.pack ? p.comp_of[s] : 0;
   if (p.pack && c.x == (T)0) return;  // zero strength contributes nothing
-  emit_records<T>(a, g, grid, comp, scatter != 0, cursor, starts, recs, str, c, nullptr, 0, cap,
+  emit_records<T>(a, g, grid, comp, kScatter, cursor, starts, recs, str, c, nullptr, 0, cap,
                   err);
 }
 
@@ -1097,6 +1101,8 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
   // job's stream waits for the second lane at the end
   const bool two = j->lane2 && !prof && count > 1;
   cudaStream_t const main_s = j->s;
+  // unit strengths (no centre phase, no spatial window) are implied, not stored
+  const bool unit_str = !j->pa.has_qc && !j->pa.window;
   if (two) {
     MPSQ_CUDA_TRY(cudaEventRecord(j->fork, main_s));
     MPSQ_CUDA_TRY(cudaStreamWaitEvent(j->s2, j->fork, 0));
@@ -1107,23 +1113,23 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     int* const counts = odd ? j->counts2 : j->counts;
     int* const starts = odd ? j->starts2 : j->starts;
     void* const recs = odd ? j->recs2 : j->recs;
-    void* const str = odd ? j->str2 : j->str;
+    void* const str = unit_str ? nullptr : (odd ? j->str2 : j->str);
     void* const fine = odd ? j->fine2 : j->fine;
     float2* const b1 = odd ? j->b1_2 : j->b1;
     const float4* frame = j->traj + (size_t)t * j->d.n_atoms_frame;
     if (mark(0)) return MPSQ_ERR_CUDA;
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 0, counts, starts,
-                                          (R*)recs, (C*)str, j->cap, j->err);
+      job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, counts, starts,
+                                                 (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
     int rc = launch_scan<T>(counts, starts, nkeys, s);
     if (rc) return rc;
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, 1, counts, starts,
-                                          (R*)recs, (C*)str, j->cap, j->err);
+      job_bin_kernel<T, true><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, counts, starts,
+                                                (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
     if (mark(1)) return MPSQ_ERR_CUDA;

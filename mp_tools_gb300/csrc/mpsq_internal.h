@@ -198,9 +198,12 @@ __device__ __forceinline__ void split_cell_f2(F2 g, int nf, float inv_nf, int w,
 }
 
 // Emits the halo copies of one point whose support starts at cell s[k] with offset d[k]:
-// one record per tile its w-cell support touches (at most 2 per dimension, periodic).
+// one record per tile its w-cell support touches (at most 2 per dimension, periodic, since
+// every tile is at least w cells wide; unused dimensions have one tile of one cell).
 // Pass 0 (scatter = false) counts records per (grid, tile) key into `cursor`; pass 1 writes
-// them at starts[key] + slot, `cursor` having been zeroed between the passes.
+// them at starts[key] + slot, `cursor` having been zeroed between the passes.  The up to 8
+// candidate tiles are handled in phases (keys, then all cursor atomics, then all stores) so
+// that the atomics' round trips overlap instead of following one another.
 template <typename T>
 __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3], const T d_in[3],
                                            int keygrid, int comp, bool scatter, int* cursor,
@@ -209,50 +212,66 @@ __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3
                                            typename Cplx<T>::type* str_out,
                                            typename Cplx<T>::type strength, int* idx_out,
                                            int src_index, int64_t cap, int* err) {
-  int i0[3], tlo[3], thi[3];
+  int tlo[3], two[3], wrap_lo[3], wrap_hi[3], loc_lo[3];
   T d[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (k < a.dim) {
       const int s = s_in[k];        // first cell of the support
       const int e = s + a.w - 1;    // last cell
-      i0[k] = s;
       d[k] = d_in[k];
       tlo[k] = s >> a.tshift[k];    // floor division: >= -1 since s >= -w and tile >= w
-      thi[k] = e >> a.tshift[k];    // <= ntile since e < nf + tile
+      two[k] = (e >> a.tshift[k]) != tlo[k];   // second tile tlo + 1 <= ntile since e < nf + tile
+      const int nt = a.ntile[k];
+      wrap_lo[k] = tlo[k] < 0 ? tlo[k] + nt : tlo[k];
+      wrap_hi[k] = tlo[k] + 1 >= nt ? tlo[k] + 1 - nt : tlo[k] + 1;
+      loc_lo[k] = s - (tlo[k] << a.tshift[k]);      // local start in the first tile
     } else {
-      i0[k] = 0;
       d[k] = (T)0;
-      tlo[k] = thi[k] = 0;
+      tlo[k] = two[k] = wrap_lo[k] = wrap_hi[k] = loc_lo[k] = 0;
     }
   }
-  for (int tz = tlo[2]; tz <= thi[2]; ++tz) {
-    const int wz = tz < 0 ? tz + a.ntile[2] : (tz >= a.ntile[2] ? tz - a.ntile[2] : tz);
-    const int lz = i0[2] - (tz << a.tshift[2]);
-    for (int ty = tlo[1]; ty <= thi[1]; ++ty) {
-      const int wy = ty < 0 ? ty + a.ntile[1] : (ty >= a.ntile[1] ? ty - a.ntile[1] : ty);
-      const int ly = i0[1] - (ty << a.tshift[1]);
-      for (int tx = tlo[0]; tx <= thi[0]; ++tx) {
-        const int wx = tx < 0 ? tx + a.ntile[0] : (tx >= a.ntile[0] ? tx - a.ntile[0] : tx);
-        const int lx = i0[0] - (tx << a.tshift[0]);
-        const int64_t key = (int64_t)keygrid * a.n_tiles + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx;
-        const int slot = atomicAdd(&cursor[key], 1);
-        if (!scatter) continue;
-        const int64_t pos = (int64_t)starts[key] + slot;
-        if (pos >= (int64_t)starts[key + 1] || pos >= cap) {
-          atomicOr(err, 1);
-          continue;
-        }
-        typename RecOf<T>::type r;
-        r.dx = d[0];
-        r.dy = d[1];
-        r.dz = d[2];
-        r.packed = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
-        recs[pos] = r;
-        if (str_out) str_out[pos] = strength;
-        if (idx_out) idx_out[pos] = src_index;
-      }
+  const int64_t gbase = (int64_t)keygrid * a.n_tiles;
+  int64_t key[8];
+  int slot[8];
+  int packed[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ix = c & 1, iy = (c >> 1) & 1, iz = c >> 2;
+    if ((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2])) continue;
+    const int wx = ix ? wrap_hi[0] : wrap_lo[0];
+    const int wy = iy ? wrap_hi[1] : wrap_lo[1];
+    const int wz = iz ? wrap_hi[2] : wrap_lo[2];
+    const int lx = loc_lo[0] - (ix << a.tshift[0]);
+    const int ly = loc_lo[1] - (iy << a.tshift[1]);
+    const int lz = loc_lo[2] - (iz << a.tshift[2]);
+    key[c] = gbase + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx;
+    packed[c] = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
+  }
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ix = c & 1, iy = (c >> 1) & 1, iz = c >> 2;
+    if ((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2])) continue;
+    slot[c] = atomicAdd(&cursor[key[c]], 1);
+  }
+  if (!scatter) return;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ix = c & 1, iy = (c >> 1) & 1, iz = c >> 2;
+    if ((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2])) continue;
+    const int64_t pos = (int64_t)starts[key[c]] + slot[c];
+    if (pos >= (int64_t)starts[key[c] + 1] || pos >= cap) {
+      atomicOr(err, 1);
+      continue;
     }
+    typename RecOf<T>::type r;
+    r.dx = d[0];
+    r.dy = d[1];
+    r.dz = d[2];
+    r.packed = packed[c];
+    recs[pos] = r;
+    if (str_out) str_out[pos] = strength;
+    if (idx_out) idx_out[pos] = src_index;
   }
 }
 

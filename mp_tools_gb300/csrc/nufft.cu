@@ -170,39 +170,65 @@ __global__ void bin_plan_kernel(int64_t nj, const T* __restrict__ x, const T* __
                   cap, err);
 }
 
-// Exclusive scan of n counts into starts[0..n], one CTA of 1024 threads.
-__global__ void scan_kernel(const int* __restrict__ counts, int* __restrict__ starts, int64_t n) {
-  __shared__ long long warp_sums[32];
-  const int nt = blockDim.x;
+// Exclusive scan of n counts into starts[0..n], one CTA of kScanThreads threads: the counts
+// pass through shared memory in spans of kScanThreads * kScanPer (coalesced loads and
+// stores), each thread scanning kScanPer consecutive entries of a span, with a running carry.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 8;
+__global__ void __launch_bounds__(kScanThreads)
+    scan_kernel(const int* __restrict__ counts, int* __restrict__ starts, int64_t n) {
+  __shared__ int buf[kScanThreads * kScanPer];
+  __shared__ long long warp_sums[kScanThreads / 32];
   const int tid = threadIdx.x;
-  int64_t chunk = (n + nt - 1) / nt;
-  int64_t lo = tid * chunk, hi = min(n, lo + chunk);
-  long long s = 0;
-  for (int64_t i = lo; i < hi; ++i) s += counts[i];
-  // block exclusive scan of s
-  long long v = s;
   const int lane = tid & 31, wid = tid >> 5;
-  for (int o = 1; o < 32; o <<= 1) {
-    long long t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  if (lane == 31) warp_sums[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    long long w = lane < (nt >> 5) ? warp_sums[lane] : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      long long t = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += t;
+  constexpr int span = kScanThreads * kScanPer;
+  long long carry = 0;
+  for (int64_t base = 0; base < n; base += span) {
+    for (int i = tid; i < span; i += kScanThreads) {
+      const int64_t g = base + i;
+      buf[i] = g < n ? counts[g] : 0;
     }
-    warp_sums[lane] = w;
+    __syncthreads();
+    int v[kScanPer];
+    long long sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+      v[k] = buf[tid * kScanPer + k];
+      sum += v[k];
+    }
+    long long incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      long long w = warp_sums[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      warp_sums[lane] = w;
+    }
+    __syncthreads();
+    long long excl = carry + incl - sum + (wid > 0 ? warp_sums[wid - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+      buf[tid * kScanPer + k] = (int)excl;
+      excl += v[k];
+    }
+    carry += warp_sums[kScanThreads / 32 - 1];
+    __syncthreads();
+    for (int i = tid; i < span; i += kScanThreads) {
+      const int64_t g = base + i;
+      if (g < n) starts[g] = buf[i];
+    }
+    __syncthreads();   // buf and warp_sums are rewritten by the next span
   }
-  __syncthreads();
-  long long excl = v - s + (wid > 0 ? warp_sums[wid - 1] : 0);
-  for (int64_t i = lo; i < hi; ++i) {
-    starts[i] = (int)excl;
-    excl += counts[i];
-  }
-  if (tid == nt - 1) starts[n] = (int)(excl);
+  if (tid == 0) starts[n] = (int)carry;
 }
 
 template <typename T>
@@ -252,7 +278,13 @@ __global__ void __launch_bounds__(NT)
   const int r0 = starts[key], r1 = starts[key + 1];
   for (int r = r0 + tid; r < r1; r += NT) {
     const auto rec = recs[r];
-    C c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+    C c;  // a null strength array means unit strengths
+    if (cv) {
+      c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+    } else {
+      c.x = (T)1;
+      c.y = (T)0;
+    }
     const int lx = (rec.packed & 0xff) - 64;
     const int ly = ((rec.packed >> 8) & 0xff) - 64;
     const int lz = ((rec.packed >> 16) & 0xff) - 64;
@@ -349,7 +381,7 @@ __global__ void __launch_bounds__(256)
     if (tid < n) {  // stage one record per thread
       const int r = c0 + tid;
       const RecF rec = recs[r];
-      const float2 c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+      const float2 c = !cv ? make_float2(1.0f, 0.0f) : idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
       const int lx = (rec.packed & 0xff) - 64;
       const int ly = ((rec.packed >> 8) & 0xff) - 64;
       const int lz = ((rec.packed >> 16) & 0xff) - 64;
@@ -495,7 +527,7 @@ __global__ void fft_radix2_kernel(double2* __restrict__ data, int n, int logn, i
 // ------------------------------------------------------------------------- host helpers
 template <typename T>
 int launch_scan(const int* counts, int* starts, int64_t n, cudaStream_t s) {
-  scan_kernel<<<1, 1024, 0, s>>>(counts, starts, n);
+  scan_kernel<<<1, kScanThreads, 0, s>>>(counts, starts, n);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
@@ -549,7 +581,7 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
 }
 
 // Spread records binned under keys [0, ngrid*n_tiles) into `ngrid` grids (job pipeline:
-// strengths per record, no gather).
+// strengths per record, no gather; str == nullptr: every strength is 1).
 template <typename T>
 int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,

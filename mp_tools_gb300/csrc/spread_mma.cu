@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(256, 3)
     if (tid < n) {
       const int r = c0 + tid;
       rec = recs[r];
-      sv = (idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r]).x;
+      sv = !cv ? 1.0f : (idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r]).x;
       const int lz = ((rec.packed >> 16) & 0xff) - 64;
       const int comp = (rec.packed >> 24) & 1;
       k = comp * K1 + min(max(lz + W - 1, 0), K1 - 1);
