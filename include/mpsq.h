@@ -248,6 +248,19 @@ int mpsq_job_radial_hist(mpsq_job* job, const double* a_cell_inv, const double* 
                          double q_step, double q_range, int32_t n_hist, double amp_scale,
                          double* out, int host);
 
+/* mp_sqom's speckle filter of a finished map (code/src/mp_sqom56.f90:1531-1570), applied by
+ * the reference when s_trig > 0 before the map's (sum N)^2 / t_step normalisation.  The map is
+ * n_fast x n_slow floats (n_fast contiguous): walking the flattened map with wrap-around
+ * neighbours, a value below min(left, right) / s_trig becomes that minimum and a value above
+ * s_trig * max(left, right) that maximum, left being the already filtered predecessor and
+ * right the unfiltered successor; perpendicular != 0 (E=const, total and I(Q,t) plane maps)
+ * repeats the walk over the transposed map, perpendicular = 0 is the E(Q) cut
+ * (n_fast = frequencies).  Bit-identical to the sequential walk.  The result is multiplied
+ * by post_scale.  host != 0: map is a host array, else a device array (in place, on
+ * `stream`).  Synchronous.  Replaces the filter loops of code/src/mp_sqom56.f90:1541-1567. */
+int mpsq_speckle_filter(float* map, int64_t n_fast, int64_t n_slow, float s_trig,
+                        int32_t perpendicular, float post_scale, int32_t host, void* stream);
+
 /* Synchronise the job's stream. */
 int mpsq_job_sync(mpsq_job* job);
 

@@ -32,7 +32,7 @@ EXPORTS = [
     "mpsq_job_sqw_gauss", "mpsq_job_sync",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
     "mpsq_version", "mpsq_launch_count",
-    "mpsq_nufft2d1_noalloc",
+    "mpsq_nufft2d1_noalloc", "mpsq_speckle_filter",
 ]
 
 
@@ -130,6 +130,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_version": (C.c_char_p, []),
         "mpsq_launch_count": (i64, []),
         "mpsq_nufft2d1_noalloc": (C.c_int, [i64, vp, vp, vp, C.c_int, dbl, i64, i64, vp, vp]),
+        "mpsq_speckle_filter": (C.c_int, [vp, i64, i64, C.c_float, i32, C.c_float, i32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

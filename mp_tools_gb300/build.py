@@ -17,7 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libmpsq.so"
-SOURCES = ["nufft.cu", "spread_mma.cu", "job.cu", "timeaxis.cu", "dropin.cu"]
+SOURCES = ["nufft.cu", "spread_mma.cu", "job.cu", "timeaxis.cu", "dropin.cu", "maps.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "--expt-relaxed-constexpr"]

@@ -401,24 +401,46 @@ class SqomJob:
     def norm2(self) -> float:
         return float(sum(self.species_counts)) ** 2
 
-    def sq_total(self, normalize: bool = True, out=None) -> np.ndarray:
-        """Total S(Q) = <|cs|^2>_t / (sum N_j)^2 (:1381-1387, :1573-1574)."""
+    def sq_total(self, normalize: bool = True, out=None, s_trig: float = 0.0) -> np.ndarray:
+        """Total S(Q) = <|cs|^2>_t / (sum N_j)^2 (:1381-1387, :1573-1574); s_trig > 0 applies
+        the speckle filter before the (sum N)^2 norm (:1531-1570, plane grids)."""
         n2 = self.norm2() if normalize else 1.0
         host = out is None or not hasattr(out, "is_cuda")
         res = np.empty(self.grid.n_modes, f32) if out is None else out
+        if s_trig > 0:
+            self._plane_shape("speckle filter")
+            check(_lib.load().mpsq_job_sq_total(self._h, 1.0, C.c_void_p(ptr(res)), int(host)), "sq_total")
+            return self._speckle(res, s_trig, False, 1.0 / n2, host)
         check(_lib.load().mpsq_job_sq_total(self._h, n2, C.c_void_p(ptr(res)), int(host)), "sq_total")
         return res
 
+    def _plane_shape(self, what):
+        if self.grid.n_q[2] != 1:
+            raise ValueError(f"{what}: defined on plane (2D) Q grids only, got {self.grid.n_q}")
+        return self.grid.n_q[1], self.grid.n_q[0]
+
+    def _speckle(self, res, s_trig, dispersion, post_scale, host=True):
+        """Speckle filter (:1531-1570) of a map in place, then the remaining normalisation."""
+        n_slow, n_fast = res.shape if dispersion else self._plane_shape("speckle filter")
+        check(_lib.load().mpsq_speckle_filter(C.c_void_p(ptr(res)), int(n_fast), int(n_slow),
+                                              float(s_trig), int(not dispersion), float(post_scale),
+                                              int(host), None), "speckle_filter")
+        return res
+
     def sqw_econst(self, taxis: TimeAxis, j_freq: int, q2_norm=None, normalize=True,
-                   t_wind=None, atom_pair=None) -> np.ndarray:
+                   t_wind=None, atom_pair=None, s_trig: float = 0.0) -> np.ndarray:
         """E=const map for 1-based bin j_freq (:1437-1478), normalised as :1527, :1575-1576.
         atom_pair=(a, b): the map of the raw amplitudes of species a + b (0-based; :1460-1464;
-        needs store_species), where q2_norm does not apply."""
+        needs store_species), where q2_norm does not apply.  s_trig > 0: speckle filter
+        (:1531-1570) between the two normalisations, as the reference applies it."""
         w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
         scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
-        if normalize:
-            scale *= taxis.t_step / self.norm2()
+        post = taxis.t_step / self.norm2() if normalize else 1.0
+        if s_trig > 0:
+            self._plane_shape("speckle filter")
+        else:
+            scale *= post
         res = np.empty(self.grid.n_modes, f32)
         L = _lib.load()
         if atom_pair is None:
@@ -429,19 +451,21 @@ class SqomJob:
             check(L.mpsq_job_sqw_econst_pair(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
                                              int(atom_pair[0]), int(atom_pair[1]), scale,
                                              C.c_void_p(ptr(res)), 1), "sqw_econst_pair")
-        return res
+        return self._speckle(res, s_trig, False, post) if s_trig > 0 else res
 
     def sqw_dispersion(self, taxis: TimeAxis, q_index, n_freq=None, q2_norm=None,
-                       normalize=True, t_wind=None, atom_pair=None) -> np.ndarray:
+                       normalize=True, t_wind=None, atom_pair=None, s_trig: float = 0.0) -> np.ndarray:
         """E(Q) cut along pixel indices q_index (:1480-1517); returns (n_path, n_freq).
-        atom_pair=(a, b): the cut of the raw amplitudes of species a + b (:1494-1499)."""
+        atom_pair=(a, b): the cut of the raw amplitudes of species a + b (:1494-1499).
+        s_trig > 0: speckle filter along the frequencies (:1531-1548)."""
         w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
         qi = np.ascontiguousarray(q_index, np.int64)
         n_freq = taxis.n_freq_max if n_freq is None else n_freq
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
         scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
-        if normalize:
-            scale *= taxis.t_step / self.norm2()
+        post = taxis.t_step / self.norm2() if normalize else 1.0
+        if not s_trig > 0:
+            scale *= post
         res = np.empty((len(qi), n_freq), f32)
         L = _lib.load()
         if atom_pair is None:
@@ -453,29 +477,35 @@ class SqomJob:
                                                  C.c_void_p(ptr(qi)), n_freq, int(atom_pair[0]),
                                                  int(atom_pair[1]), scale, C.c_void_p(ptr(res)), 1),
                   "sqw_dispersion_pair")
-        return res
+        return self._speckle(res, s_trig, True, post) if s_trig > 0 else res
 
-    def iqt(self, n_int: int, lag: int, q2_norm=None, normalize=True) -> np.ndarray:
+    def iqt(self, n_int: int, lag: int, q2_norm=None, normalize=True,
+            s_trig: float = 0.0) -> np.ndarray:
         """I(Q,t) map at a time lag of `lag` frames (the j_sq /= 1 branch, :1467-1472),
-        normalised by (sum N)^2 (:1573-1574)."""
+        normalised by (sum N)^2 (:1573-1574); s_trig > 0: speckle filter before the norm."""
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
-        scale = 1.0 / self.norm2() if normalize else 1.0
+        post = 1.0 / self.norm2() if normalize else 1.0
+        if s_trig > 0:
+            self._plane_shape("speckle filter")
+        scale = 1.0 if s_trig > 0 else post
         res = np.empty(self.grid.n_modes, f32)
         check(_lib.load().mpsq_job_iqt(self._h, int(n_int), int(lag), C.c_void_p(ptr(q2)), scale,
                                        C.c_void_p(ptr(res)), 1), "iqt")
-        return res
+        return self._speckle(res, s_trig, False, post) if s_trig > 0 else res
 
-    def iqt_dispersion(self, n_int: int, q_index, q2_norm=None, normalize=True) -> np.ndarray:
+    def iqt_dispersion(self, n_int: int, q_index, q2_norm=None, normalize=True,
+                       s_trig: float = 0.0) -> np.ndarray:
         """I(Q,t) along pixel indices q_index for lags 0..n_frames-n_int (:1504-1510, :699);
-        returns (n_path, n_frames - n_int + 1)."""
+        returns (n_path, n_frames - n_int + 1); s_trig > 0: speckle filter along the lags."""
         qi = np.ascontiguousarray(q_index, np.int64)
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
-        scale = 1.0 / self.norm2() if normalize else 1.0
+        post = 1.0 / self.norm2() if normalize else 1.0
+        scale = 1.0 if s_trig > 0 else post
         res = np.empty((len(qi), self.n_frames - int(n_int) + 1), f32)
         check(_lib.load().mpsq_job_iqt_dispersion(self._h, int(n_int), len(qi), C.c_void_p(ptr(qi)),
                                                   C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
               "iqt_dispersion")
-        return res
+        return self._speckle(res, s_trig, True, post) if s_trig > 0 else res
 
     def sqw_gauss(self, fwhm_frames=None, n_freq=None, t_step=1.0, q2_norm=None, normalize=True,
                   out=None) -> np.ndarray:
@@ -494,6 +524,21 @@ class SqomJob:
         check(_lib.load().mpsq_job_sqw_gauss(self._h, float(fwhm), n_freq, C.c_void_p(ptr(q2)),
                                              scale, C.c_void_p(ptr(res)), int(host)), "sqw_gauss")
         return res
+
+
+def speckle_filter(cs_plot, s_trig: float, dispersion: bool = False,
+                   post_scale: float = 1.0) -> np.ndarray:
+    """mp_sqom's speckle filter (code/src/mp_sqom56.f90:1531-1570) on the GPU, for a finished
+    host map: a plane map as (n_qy, n_qx) (qx contiguous; two walks, the second over the
+    transposed map) or an E(Q) / I(Q,t) cut as (n_path, n_freq) (dispersion=True; one walk
+    along the frequencies).  Returns a new float32 array times post_scale."""
+    m = np.array(cs_plot, dtype=f32, copy=True, order="C")
+    if m.ndim != 2:
+        raise ValueError(f"speckle filter: a 2D map is needed, got shape {m.shape}")
+    check(_lib.load().mpsq_speckle_filter(C.c_void_p(m.ctypes.data), m.shape[1], m.shape[0],
+                                          float(s_trig), int(not dispersion), float(post_scale),
+                                          1, None), "speckle_filter")
+    return m
 
 
 _rt = None

@@ -10,6 +10,7 @@ the reference lines it follows (paths relative to the MP_TOOLS tree):
   econst           code/src/mp_sqom56.f90:1437-1478  sliding-window E=const map
   dispersion       code/src/mp_sqom56.f90:1480-1517  E(Q) cut, FFT per start frame
   gauss_spectrum   whole-run Gaussian window + one DFT per Q (the benchmark's time transform)
+  speckle_filter   code/src/mp_sqom56.f90:1531-1570  sequential speckle walk on a finished map
   xray_ff          code/src/mp_sqom56.f90:919-936 (and mp_sql56.f90:1048-1058 convention)
 """
 from __future__ import annotations
@@ -181,3 +182,38 @@ def gauss_spectrum(cs, fwhm, n_freq, q2_norm=None, scale=1.0):
     g = gauss_window(x.shape[0], fwhm)[:, None]
     X = np.fft.fft(g * x, axis=0)[:n_freq]
     return np.abs(X) ** 2 * scale
+
+
+def _speckle_walk(csp, s_trig):
+    """One walk of :1541-1548 over a flat float32 array, in place and in the reference's
+    order: the left neighbour is already filtered, the right one not (except that the last
+    value's right neighbour is the filtered first value); wrap-around at both ends."""
+    s = np.float32(s_trig)
+    n = csp.size
+    for i2 in range(n):
+        a = csp[i2 - 1]                    # i1 = i2 - 1, wrapping to the last value
+        b = csp[(i2 + 1) % n]              # i3 = i2 + 1, wrapping to the (filtered) first
+        lo, hi = min(a, b), max(a, b)
+        if csp[i2] < np.float32(lo / s):
+            csp[i2] = lo
+        if csp[i2] > np.float32(s * hi):
+            csp[i2] = hi
+
+
+def speckle_filter(cs_plot, s_trig, dispersion=False):
+    """The speckle filter of :1531-1570 on a finished map (float32).
+
+    Plane maps (dispersion False) are given as an (n_qy, n_qx) array, i.e. the reference's
+    cs_plot(n_qx, n_qy) with qx contiguous: a walk over the flattened map, then a walk over
+    the transposed map.  E(Q) cuts (dispersion True) are given as (n_qdisp, n_freq) with the
+    frequency contiguous, the reference's cs_plot(n_freq_max, n_qdisp) after :1538: one walk."""
+    m = np.array(cs_plot, dtype=np.float32, copy=True)
+    shape = m.shape
+    flat = m.reshape(-1)
+    _speckle_walk(flat, s_trig)
+    if not dispersion:
+        t = np.ascontiguousarray(flat.reshape(shape).T)
+        tf = t.reshape(-1)
+        _speckle_walk(tf, s_trig)
+        return np.ascontiguousarray(tf.reshape(t.shape).T)
+    return flat.reshape(shape)
