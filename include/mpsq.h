@@ -261,6 +261,21 @@ int mpsq_job_radial_hist(mpsq_job* job, const double* a_cell_inv, const double* 
 int mpsq_speckle_filter(float* map, int64_t n_fast, int64_t n_slow, float s_trig,
                         int32_t perpendicular, float post_scale, int32_t host, void* stream);
 
+/* One-phonon mode (mp_sqom's j_oneph = 1, code/src/mp_sqom56.f90:1037-1098; "for verification"),
+ * replacing mpsq_job_transform for frames [first, first+count): per species, the in-plane
+ * displacements d = r - at_base - cell (+ n_row/2) summed per cell column into u_x, u_y on the
+ * n_row x n_row cell grid, 2D FFT (exp(-i), unscaled) / n_row, and for Q pixel
+ * ((ii-1) n_row + k, (jj-1) n_row + l) of the n_bz x n_bz zones
+ *   A_j = exp(-2 pi i (q_x b_x + q_y b_y)) (q_x u_qx(kk,ll) + q_y u_qy(kk,ll)),
+ *   q_x = qx_min + (ii-1) + (k-1)/n_row, kk = mod(n_row frac(qx_min) + k, n_row) (0 -> n_row),
+ * then the job's species weights, mask and window norm into cs(t, Q) (pixels beyond the zones:
+ * 0).  plane 1 = (hk0): b = (b1, b2); plane 2 = (hhl): k from c1 + c2, l = c3,
+ * d_x = (d1 + d2 + 2)/sqrt 2, d_y = d3 + 1, b = (b1 + b2, b3).  CELL input on a Q plane with
+ * n_row(1) = n_row(2) (= n_row(3) on (hhl)); cell indices set first.  at_base: host
+ * float[n_species][3] (the frame header's basis positions).  Asynchronous on the job's stream. */
+int mpsq_job_transform_onephonon(mpsq_job* job, int32_t first, int32_t count, int32_t plane,
+                                 int32_t n_bz, float qx_min, float qy_min, const float* at_base);
+
 /* Synchronise the job's stream. */
 int mpsq_job_sync(mpsq_job* job);
 

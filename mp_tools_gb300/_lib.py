@@ -32,7 +32,7 @@ EXPORTS = [
     "mpsq_job_sqw_gauss", "mpsq_job_sync",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
     "mpsq_version", "mpsq_launch_count",
-    "mpsq_nufft2d1_noalloc", "mpsq_speckle_filter",
+    "mpsq_nufft2d1_noalloc", "mpsq_speckle_filter", "mpsq_job_transform_onephonon",
 ]
 
 
@@ -131,6 +131,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_launch_count": (i64, []),
         "mpsq_nufft2d1_noalloc": (C.c_int, [i64, vp, vp, vp, C.c_int, dbl, i64, i64, vp, vp]),
         "mpsq_speckle_filter": (C.c_int, [vp, i64, i64, C.c_float, i32, C.c_float, i32, vp]),
+        "mpsq_job_transform_onephonon": (C.c_int, [vp, i32, i32, i32, i32, C.c_float, C.c_float, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

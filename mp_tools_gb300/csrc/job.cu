@@ -145,6 +145,11 @@ struct mpsq_job {
   void* recs2 = nullptr;
   void* str2 = nullptr;
   float2* b1_2 = nullptr;
+  // one-phonon mode: displacement fields (n_species x 2 x n_row2 x n_row1, job precision)
+  void* oneph_u = nullptr;
+  float* oneph_base = nullptr;
+  cufftHandle oneph_fft = 0;
+  bool have_oneph_fft = false;
 };
 
 namespace mpsq {
@@ -362,6 +367,129 @@ __global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
         va.y = G.y * corr * WP<T>::wnorm(w);
         cs_species_frame[(int64_t)sa * nm + q] = va;
       }
+    }
+  }
+  C out;
+  out.x = accr * WP<T>::wnorm(w);
+  out.y = acci * WP<T>::wnorm(w);
+  cs_frame[q] = out;
+}
+
+// -------------------------------------------------------------------- one-phonon mode
+// mp_sqom's j_oneph = 1 branch (code/src/mp_sqom56.f90:1037-1098): per species, the in-plane
+// displacements of the atoms are summed over the cell columns of the plane into two real
+// fields u_x(k, l), u_y(k, l) on the n_row x n_row cell grid, Fourier transformed (forward,
+// exp(-i), unscaled) and divided by n_row, and every Q pixel of the n_bz x n_bz zones takes
+// A_j(Q) = exp(-2 pi i q . b_j) (q_x u_qx + q_y u_qy) at the zone-folded cell frequency.
+// Plane 1 is (hk0): k, l = cell indices 1, 2, d = r - b - cell + n_row/2.  Plane 2 is (hhl):
+// k = mod(c1 - 1 + c2 - 1, n_row) + 1, l = c3, d_x = (d1 + d2 + 2)/sqrt 2, d_y = d3 + 1
+// (the reference's "+1" on this plane kept).  Displacements in FP32 in the reference's order.
+
+// u: [n_species][2][n2][n1] complex, zeroed; atoms at exactly (0,0,0) are vacancies (:1049).
+template <typename T>
+__global__ void oneph_scatter_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
+                                     PrepArgs p, int plane, const float* __restrict__ base,
+                                     int n1, int n2, typename Cplx<T>::type* __restrict__ u) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.n_atoms_frame) return;
+  if (j < p.species_offset[0] || j >= p.species_offset[p.n_species]) return;
+  int s = 0;
+  while (s + 1 < p.n_species && j >= p.species_offset[s + 1]) ++s;
+  if (p.group_of[s] < 0) return;  // masked species are not transformed
+  const float4 r = frame[j];
+  if (r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) return;
+  const int4 c = at_ind[j];
+  const float b0 = base[3 * s], b1 = base[3 * s + 1], b2 = base[3 * s + 2];
+  int k, l;
+  float dx, dy;
+  if (plane == 1) {
+    k = c.x;
+    l = c.y;
+    dx = __fadd_rn(__fsub_rn(__fsub_rn(r.x, b0), (float)c.x), (float)(p.n_row[0] / 2));
+    dy = __fadd_rn(__fsub_rn(__fsub_rn(r.y, b1), (float)c.y), (float)(p.n_row[1] / 2));
+  } else {
+    const int per = (p.n_row[0] + p.n_row[1]) / 2;
+    k = ((c.x - 1 + c.y - 1) % per + per) % per + 1;
+    l = c.z;
+    float t = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(r.x, b0), (float)c.x), (float)(p.n_row[0] / 2)), 1.0f);
+    t = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fadd_rn(t, r.y), b1), (float)c.y), (float)(p.n_row[1] / 2)), 1.0f);
+    dx = __fdiv_rn(t, sqrtf(2.0f));
+    dy = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(r.z, b2), (float)c.z), (float)(p.n_row[2] / 2)), 1.0f);
+  }
+  if (k < 1 || k > n1 || l < 1 || l > n2) return;  // outside the cell grid
+  const int64_t cell = (int64_t)(l - 1) * n1 + (k - 1);
+  const int64_t plane_sz = (int64_t)n1 * n2;
+  atomicAdd(&u[(2 * (int64_t)s) * plane_sz + cell].x, (T)dx);
+  atomicAdd(&u[(2 * (int64_t)s + 1) * plane_sz + cell].x, (T)dy);
+}
+
+// One thread per Q pixel (i, j) of the m0 x m1 plane; pixels beyond the n_bz zones (which the
+// reference never writes) are zero.  Species weights, mask and window norm as the NUFFT path.
+template <typename T>
+__global__ void oneph_expand_kernel(const typename Cplx<T>::type* __restrict__ u, PrepArgs p,
+                                    int plane, const float* __restrict__ base, int n1, int n2,
+                                    int m0, int m1, int n_bz, float qx_min, float qy_min,
+                                    int nqx_min, int nqy_min, WeightArgs w,
+                                    typename Cplx<T>::type* __restrict__ cs_frame,
+                                    typename Cplx<T>::type* __restrict__ cs_species_frame) {
+  using C = typename Cplx<T>::type;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int jq = blockIdx.y;
+  if (i >= m0) return;
+  const int64_t q = (int64_t)jq * m0 + i;
+  const int64_t nm = (int64_t)m0 * m1;
+  const int ii = i / n1, jj = jq / n2;
+  const bool inside = ii < n_bz && jj < n_bz;
+  const int k = i - ii * n1 + 1, l = jq - jj * n2 + 1;
+  // q_x = qx_min + (ii - 1) + (k - 1) / n_row in FP32 (1-based ii there)
+  const float qx = __fadd_rn(__fadd_rn(qx_min, (float)ii), __fdiv_rn((float)(k - 1), (float)n1));
+  const float qy = __fadd_rn(__fadd_rn(qy_min, (float)jj), __fdiv_rn((float)(l - 1), (float)n2));
+  int kk = (nqx_min + k) % n1, ll = (nqy_min + l) % n2;
+  if (kk == 0) kk = n1;
+  if (ll == 0) ll = n2;
+  const int64_t cell = (int64_t)(ll - 1) * n1 + (kk - 1);
+  const int64_t plane_sz = (int64_t)n1 * n2;
+  T s2 = 0;
+  if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+    const int kx = i - m0 / 2, ky = jq - m1 / 2;
+    T qv[3];
+    for (int b = 0; b < 3; ++b)
+      qv[b] = WP<T>::q0(w, b) + (T)kx * WP<T>::qs(w, 0, b) + (T)ky * WP<T>::qs(w, 1, b);
+    s2 = WP<T>::kappa(w) * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + WP<T>::extra(w));
+  }
+  const float tpi = 6.28318530717958647692f;
+  T accr = 0, acci = 0;
+  for (int s = 0; s < p.n_species; ++s) {
+    if (p.group_of[s] < 0) continue;
+    C a;
+    a.x = (T)0;
+    a.y = (T)0;
+    if (inside) {
+      const C ux = u[(2 * (int64_t)s) * plane_sz + cell];
+      const C uy = u[(2 * (int64_t)s + 1) * plane_sz + cell];
+      const T fx = (T)qx / (T)n1, fy = (T)qy / (T)n2;
+      const T vr = fx * ux.x + fy * uy.x, vi = fx * ux.y + fy * uy.y;
+      const float b0 = base[3 * s], b1 = base[3 * s + 1], b2 = base[3 * s + 2];
+      const float dot = plane == 1 ? __fadd_rn(__fmul_rn(qx, b0), __fmul_rn(qy, b1))
+                                   : __fadd_rn(__fmul_rn(qx, __fadd_rn(b0, b1)), __fmul_rn(qy, b2));
+      const float arg = __fmul_rn(tpi, dot);
+      T sn, cn;
+      if constexpr (sizeof(T) == 8) {
+        sincos((double)arg, &sn, &cn);
+      } else {
+        sincosf(arg, &sn, &cn);
+      }
+      a.x = cn * vr + sn * vi;      // (cos - i sin)(vr + i vi)
+      a.y = cn * vi - sn * vr;
+    }
+    const T ws = species_weight<T>(w, s, s2);
+    accr += ws * a.x;
+    acci += ws * a.y;
+    if (w.store_species) {
+      C v;
+      v.x = a.x * WP<T>::wnorm(w);
+      v.y = a.y * WP<T>::wnorm(w);
+      cs_species_frame[(int64_t)s * nm + q] = v;
     }
   }
   C out;
@@ -781,6 +909,9 @@ static void job_free(mpsq_job* j) {
   cudaFree(j->recs2);
   cudaFree(j->str2);
   cudaFree(j->b1_2);
+  if (j->have_oneph_fft) cufftDestroy(j->oneph_fft);
+  cudaFree(j->oneph_u);
+  cudaFree(j->oneph_base);
   if (j->fork) cudaEventDestroy(j->fork);
   if (j->join) cudaEventDestroy(j->join);
   if (j->s2) cudaStreamDestroy(j->s2);
@@ -1196,6 +1327,79 @@ extern "C" int mpsq_job_transform(mpsq_job* j, int32_t first, int32_t count) {
     return fail(MPSQ_ERR_ARG, "transform: frames outside the trajectory");
   return j->d.precision == MPSQ_FP64 ? job_transform_t<double>(j, first, count)
                                      : job_transform_t<float>(j, first, count);
+}
+
+template <typename T>
+static int job_onephonon_t(mpsq_job* j, int32_t first, int32_t count, int32_t plane, int32_t n_bz,
+                           float qx_min, float qy_min) {
+  using C = typename Cplx<T>::type;
+  const int n1 = j->d.n_row[0], n2 = j->d.n_row[1];
+  const int m0 = (int)j->d.n_modes[0], m1 = (int)j->d.n_modes[1];
+  const int ns = j->d.n_species;
+  const size_t usz = (size_t)ns * 2 * n1 * n2 * sizeof(C);
+  if (!j->oneph_u) MPSQ_CUDA_TRY(cudaMalloc(&j->oneph_u, usz));
+  if (!j->have_oneph_fft) {
+    int n[2] = {n2, n1};
+    MPSQ_CUFFT_TRY(cufftPlanMany(&j->oneph_fft, 2, n, nullptr, 1, n1 * n2, nullptr, 1, n1 * n2,
+                                 sizeof(T) == 8 ? CUFFT_Z2Z : CUFFT_C2C, 2 * ns));
+    j->have_oneph_fft = true;
+  }
+  MPSQ_CUFFT_TRY(cufftSetStream(j->oneph_fft, j->s));
+  // nqx_min = n_row * (qx_min - floor(qx_min)), FP32, truncated (:1039-1040)
+  const int nqx_min = (int)(float)((float)n1 * (qx_min - std::floor(qx_min)));
+  const int nqy_min = (int)(float)((float)n2 * (qy_min - std::floor(qy_min)));
+  const int bt = 256;
+  const unsigned nb = (unsigned)((j->d.n_atoms_frame + bt - 1) / bt);
+  const int64_t nm = j->g.n_modes;
+  for (int32_t t = first; t < first + count; ++t) {
+    MPSQ_CUDA_TRY(cudaMemsetAsync(j->oneph_u, 0, usz, j->s));
+    oneph_scatter_kernel<T><<<nb, bt, 0, j->s>>>(j->traj + (size_t)t * j->d.n_atoms_frame,
+                                                  j->at_ind, j->pa, plane, j->oneph_base, n1, n2,
+                                                  (C*)j->oneph_u);
+    MPSQ_LAUNCH_CHECK();
+    if constexpr (sizeof(T) == 8) {
+      MPSQ_CUFFT_TRY(cufftExecZ2Z(j->oneph_fft, (cufftDoubleComplex*)j->oneph_u,
+                                  (cufftDoubleComplex*)j->oneph_u, CUFFT_FORWARD));
+    } else {
+      MPSQ_CUFFT_TRY(cufftExecC2C(j->oneph_fft, (cufftComplex*)j->oneph_u,
+                                  (cufftComplex*)j->oneph_u, CUFFT_FORWARD));
+    }
+    C* csf = (C*)j->cs + (size_t)t * nm;
+    C* css = j->cs_species ? (C*)j->cs_species + (size_t)t * ns * nm : nullptr;
+    oneph_expand_kernel<T><<<dim3((unsigned)((m0 + 127) / 128), (unsigned)m1), 128, 0, j->s>>>(
+        (const C*)j->oneph_u, j->pa, plane, j->oneph_base, n1, n2, m0, m1, n_bz, qx_min, qy_min,
+        nqx_min, nqy_min, j->wa, csf, css);
+    MPSQ_LAUNCH_CHECK();
+  }
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_transform_onephonon(mpsq_job* j, int32_t first, int32_t count,
+                                            int32_t plane, int32_t n_bz, float qx_min,
+                                            float qy_min, const float* at_base) {
+  if (!j || !at_base) return fail(MPSQ_ERR_ARG, "transform_onephonon: null pointer");
+  if (first < 0 || count < 0 || first + count > j->d.n_frames)
+    return fail(MPSQ_ERR_ARG, "transform_onephonon: frames outside the trajectory");
+  if (j->d.input_method != MPSQ_CELL || j->d.ndim != 2)
+    return fail(MPSQ_ERR_ARG, "transform_onephonon: CELL input on a Q plane only (the reference "
+                "turns the mode off for BULK input)");
+  if (plane != 1 && plane != 2)
+    return fail(MPSQ_ERR_ARG, "transform_onephonon: plane must be 1 (hk0) or 2 (hhl), got %d", plane);
+  const int* nr = j->d.n_row;
+  if (nr[0] != nr[1] || (plane == 2 && nr[2] != nr[0]))
+    return fail(MPSQ_ERR_ARG, "transform_onephonon: needs n_row(1) = n_row(2) (= n_row(3) on "
+                "(hhl)); the reference's index ranges mix the axes otherwise");
+  if (n_bz < 1 || (int64_t)n_bz * nr[0] > j->d.n_modes[0] || (int64_t)n_bz * nr[1] > j->d.n_modes[1])
+    return fail(MPSQ_ERR_ARG, "transform_onephonon: %d zones of %d cells exceed the %lld x %lld plane",
+                n_bz, nr[0], (long long)j->d.n_modes[0], (long long)j->d.n_modes[1]);
+  if (!j->at_ind) return fail(MPSQ_ERR_STATE, "transform_onephonon: set the cell indices first");
+  if (!j->oneph_base) MPSQ_CUDA_TRY(cudaMalloc(&j->oneph_base, sizeof(float) * 3 * MPSQ_MAX_SPECIES));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(j->oneph_base, at_base, sizeof(float) * 3 * j->d.n_species,
+                                cudaMemcpyHostToDevice, j->s));
+  // (a host-to-device copy from pageable memory has left the caller's buffer on return)
+  return j->d.precision == MPSQ_FP64
+             ? job_onephonon_t<double>(j, first, count, plane, n_bz, qx_min, qy_min)
+             : job_onephonon_t<float>(j, first, count, plane, n_bz, qx_min, qy_min);
 }
 
 extern "C" int mpsq_job_profile(mpsq_job* j, int enable) {

@@ -351,6 +351,20 @@ class SqomJob:
         count = self.n_frames - first if count is None else count
         check(_lib.load().mpsq_job_transform(self._h, first, count), "transform")
 
+    def transform_onephonon(self, j_plane: int, at_base, first: int = 0, count: int | None = None):
+        """One-phonon amplitudes instead of the NUFFT (mp_sqom's j_oneph = 1,
+        code/src/mp_sqom56.f90:1037-1098) for frames [first, first+count): j_plane 1 = (hk0),
+        2 = (hhl); at_base (n_species, 3) basis positions in cells (the frame header's at_base).
+        CELL input on a Q plane, cell indices set (set_cell_index)."""
+        g = self.grid
+        count = self.n_frames - first if count is None else count
+        base = np.ascontiguousarray(np.asarray(at_base, f32).reshape(-1, 3))
+        if base.shape[0] != len(self.species_counts):
+            raise ValueError(f"at_base: {base.shape[0]} rows for {len(self.species_counts)} species")
+        check(_lib.load().mpsq_job_transform_onephonon(
+            self._h, first, count, int(j_plane), int(round(float(g.n_bz))), float(g.q_min[0]),
+            float(g.q_min[1]), C.c_void_p(base.ctypes.data)), "transform_onephonon")
+
     def sync(self):
         check(_lib.load().mpsq_job_sync(self._h), "sync")
 

@@ -11,6 +11,7 @@ the reference lines it follows (paths relative to the MP_TOOLS tree):
   dispersion       code/src/mp_sqom56.f90:1480-1517  E(Q) cut, FFT per start frame
   gauss_spectrum   whole-run Gaussian window + one DFT per Q (the benchmark's time transform)
   speckle_filter   code/src/mp_sqom56.f90:1531-1570  sequential speckle walk on a finished map
+  one_phonon       code/src/mp_sqom56.f90:1037-1098  displacement-field (one-phonon) amplitudes
   xray_ff          code/src/mp_sqom56.f90:919-936 (and mp_sql56.f90:1048-1058 convention)
 """
 from __future__ import annotations
@@ -217,3 +218,61 @@ def speckle_filter(cs_plot, s_trig, dispersion=False):
         _speckle_walk(tf, s_trig)
         return np.ascontiguousarray(tf.reshape(t.shape).T)
     return flat.reshape(shape)
+
+
+def one_phonon(frame, at_ind, counts, at_base, n_row, n_bz, qx_min, qy_min, plane, n_q):
+    """Per-species one-phonon amplitudes of one frame (:1037-1098), shape (S, n_qy, n_qx),
+    complex128; pixels beyond the n_bz x n_bz zones are 0 (the reference leaves them unset).
+    Displacements in FP32 in the reference's order, sums and transforms in FP64."""
+    f = np.float32
+    n1, n2 = int(n_row[0]), int(n_row[1])
+    nqx, nqy = int(n_q[0]), int(n_q[1])
+    off = np.concatenate([[0], np.cumsum(counts)])
+    S = len(counts)
+    out = np.zeros((S, nqy, nqx), np.complex128)
+    qx_min, qy_min = f(qx_min), f(qy_min)
+    nqx_min = int(f(f(n1) * f(qx_min - np.floor(qx_min))))        # :1039-1040, truncation
+    nqy_min = int(f(f(n2) * f(qy_min - np.floor(qy_min))))
+    for j in range(S):
+        r = frame[off[j]:off[j + 1], :3].astype(f)
+        c = at_ind[off[j]:off[j + 1], :3].astype(np.int64)
+        b = np.asarray(at_base[j], f)
+        keep = ~((r[:, 0] == 0) & (r[:, 1] == 0) & (r[:, 2] == 0))   # vacancies (:1049)
+        r, c = r[keep], c[keep]
+        if plane == 1:                                                # :1046-1057
+            k, l = c[:, 0], c[:, 1]
+            dx = ((r[:, 0] - b[0]) - c[:, 0].astype(f)) + f(n_row[0] // 2)
+            dy = ((r[:, 1] - b[1]) - c[:, 1].astype(f)) + f(n_row[1] // 2)
+        else:                                                         # :1059-1071
+            k = np.mod(c[:, 0] - 1 + c[:, 1] - 1, (n_row[0] + n_row[1]) // 2) + 1
+            l = c[:, 2]
+            t = (((r[:, 0] - b[0]) - c[:, 0].astype(f)) + f(n_row[0] // 2)) + f(1)
+            t = ((((t + r[:, 1]) - b[1]) - c[:, 1].astype(f)) + f(n_row[1] // 2)) + f(1)
+            dx = (t / f(np.sqrt(f(2.0)))).astype(f)
+            dy = ((((r[:, 2] - b[2]) - c[:, 2].astype(f)) + f(n_row[2] // 2)) + f(1)).astype(f)
+        ux = np.zeros((n2, n1))
+        uy = np.zeros((n2, n1))
+        np.add.at(ux, (l - 1, k - 1), dx.astype(np.float64))
+        np.add.at(uy, (l - 1, k - 1), dy.astype(np.float64))
+        uqx = np.fft.fft2(ux) / n1                                    # forward exp(-i), :1075
+        uqy = np.fft.fft2(uy) / n2
+        for jj in range(int(n_bz)):
+            for ii in range(int(n_bz)):
+                kk = np.arange(1, n1 + 1)
+                ll = np.arange(1, n2 + 1)
+                qx = (f(qx_min + f(ii)) + (f(1) * (kk - 1).astype(f)) / f(n1)).astype(f)
+                qy = (f(qy_min + f(jj)) + (f(1) * (ll - 1).astype(f)) / f(n2)).astype(f)
+                ik = np.mod(nqx_min + kk, n1)
+                ik[ik == 0] = n1
+                il = np.mod(nqy_min + ll, n2)
+                il[il == 0] = n2
+                QX, QY = np.meshgrid(qx.astype(np.float64), qy.astype(np.float64))
+                IK, IL = np.meshgrid(ik - 1, il - 1)
+                if plane == 1:
+                    dot = f(qx[None, :] * b[0]) + f(qy[:, None] * b[1])
+                else:
+                    dot = f(qx[None, :] * f(b[0] + b[1])) + f(qy[:, None] * b[2])
+                arg = (f(2.0 * np.pi) * dot.astype(f)).astype(np.float64)
+                val = np.exp(-1j * arg) * (QX * uqx[IL, IK] + QY * uqy[IL, IK])
+                out[j, jj * n2:(jj + 1) * n2, ii * n1:(ii + 1) * n1] = val
+    return out
