@@ -350,19 +350,22 @@ def run_gpu(args):
     host_sq = torch.empty(sq.shape, dtype=torch.float32, pin_memory=True)
 
     def step_e2e():
-        job.transform_from_host(host_frames)    # chunked upload overlapping the transform
-        job.sq_total(out=sq)
-        job.sqw_gauss(fwhm_frames=FRAMES / 2, n_freq=n_freq, t_step=T_STEP, out=sqw)
-        host_sqw.copy_(sqw, non_blocking=True)
-        host_sq.copy_(sq, non_blocking=True)
+        # chunked upload overlapping the transform; the maps land in pinned host memory by
+        # copies that overlap the next step's transform (the job orders buffer reuse)
+        job.transform_from_host(host_frames)
+        job.sq_total(out=host_sq)
+        job.sqw_gauss(fwhm_frames=FRAMES / 2, n_freq=n_freq, t_step=T_STEP, out=host_sqw)
 
     step_e2e()
+    job.sync()
     barrier()
     e_steps = max(1, min(args.steps, 3))
     e0.record(stream)
     for _ in range(e_steps):
         step_e2e()
+    job.wait_outputs()          # every step's maps are on the host before the end event
     e1.record(stream)
+    job.sync()
     barrier()
     ms_e2e = e0.elapsed_time(e1) / e_steps
     ms_e2e = max_over_ranks(ms_e2e, dist, "cuda")

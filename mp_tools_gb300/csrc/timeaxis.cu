@@ -546,14 +546,19 @@ static int out_finish(float* out, int host, size_t n, OutBuf* b, cudaStream_t s)
   return MPSQ_OK;
 }
 
-// Small host array -> temporary device copy.
+// Small host array -> temporary device copy, stream-ordered (allocated and freed on the
+// job's stream, so that a call does not wait for the work queued before it).
 template <typename X>
 static int dev_copy(const X* h, size_t n, X** d, cudaStream_t s) {
   *d = nullptr;
   if (!h) return MPSQ_OK;
-  MPSQ_CUDA_TRY(cudaMalloc(d, std::max<size_t>(16, n * sizeof(X))));
+  MPSQ_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(d), std::max<size_t>(16, n * sizeof(X)), s));
   MPSQ_CUDA_TRY(cudaMemcpyAsync(*d, h, n * sizeof(X), cudaMemcpyHostToDevice, s));
   return MPSQ_OK;
+}
+template <typename X>
+static void dev_free(X* d, cudaStream_t s) {
+  if (d) cudaFreeAsync(d, s);
 }
 
 }  // namespace mpsq
@@ -623,8 +628,8 @@ int econst_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const float* 
   OutBuf b;
   if (!rc) rc = out_prepare(out, host, v.n_q, &b);
   if (rc) {
-    cudaFree(dw);
-    cudaFree(dq);
+    dev_free(dw, v.s);
+    dev_free(dq, v.s);
     return rc;
   }
   const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
@@ -642,9 +647,8 @@ int econst_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const float* 
   cudaError_t e = cudaGetLastError();
   rc = e == cudaSuccess ? out_finish(out, host, v.n_q, &b, v.s)
                         : fail(MPSQ_ERR_CUDA, "econst launch: %s", cudaGetErrorString(e));
-  cudaStreamSynchronize(v.s);
-  cudaFree(dw);
-  cudaFree(dq);
+  dev_free(dw, v.s);
+  dev_free(dq, v.s);
   return rc;
 }
 
@@ -666,9 +670,9 @@ int dispersion_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const flo
   OutBuf b;
   if (!rc) rc = out_prepare(out, host, (size_t)n_path * n_freq, &b);
   if (rc) {
-    cudaFree(dw);
-    cudaFree(dq);
-    cudaFree(di);
+    dev_free(dw, v.s);
+    dev_free(dq, v.s);
+    dev_free(di, v.s);
     return rc;
   }
   if (v.precision == MPSQ_FP64) {
@@ -684,10 +688,9 @@ int dispersion_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const flo
   cudaError_t e = cudaGetLastError();
   rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_path * n_freq, &b, v.s)
                         : fail(MPSQ_ERR_CUDA, "dispersion launch: %s", cudaGetErrorString(e));
-  cudaStreamSynchronize(v.s);
-  cudaFree(dw);
-  cudaFree(dq);
-  cudaFree(di);
+  dev_free(dw, v.s);
+  dev_free(dq, v.s);
+  dev_free(di, v.s);
   return rc;
 }
 }  // namespace
@@ -748,7 +751,7 @@ extern "C" int mpsq_job_iqt(mpsq_job* j, int32_t n_int, int32_t lag, const float
   OutBuf b;
   if (!rc) rc = out_prepare(out, host, v.n_q, &b);
   if (rc) {
-    cudaFree(dq);
+    dev_free(dq, v.s);
     return rc;
   }
   const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
@@ -766,8 +769,7 @@ extern "C" int mpsq_job_iqt(mpsq_job* j, int32_t n_int, int32_t lag, const float
   cudaError_t e = cudaGetLastError();
   rc = e == cudaSuccess ? out_finish(out, host, v.n_q, &b, v.s)
                         : fail(MPSQ_ERR_CUDA, "iqt launch: %s", cudaGetErrorString(e));
-  cudaStreamSynchronize(v.s);
-  cudaFree(dq);
+  dev_free(dq, v.s);
   return rc;
 }
 
@@ -790,8 +792,8 @@ extern "C" int mpsq_job_iqt_dispersion(mpsq_job* j, int32_t n_int, int32_t n_pat
   OutBuf b;
   if (!rc) rc = out_prepare(out, host, (size_t)n_path * n_lag, &b);
   if (rc) {
-    cudaFree(dq);
-    cudaFree(di);
+    dev_free(dq, v.s);
+    dev_free(di, v.s);
     return rc;
   }
   const SeriesArgs src = weighted_series(v);
@@ -808,9 +810,8 @@ extern "C" int mpsq_job_iqt_dispersion(mpsq_job* j, int32_t n_int, int32_t n_pat
   cudaError_t e = cudaGetLastError();
   rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_path * n_lag, &b, v.s)
                         : fail(MPSQ_ERR_CUDA, "iqt_dispersion launch: %s", cudaGetErrorString(e));
-  cudaStreamSynchronize(v.s);
-  cudaFree(dq);
-  cudaFree(di);
+  dev_free(dq, v.s);
+  dev_free(di, v.s);
   return rc;
 }
 
@@ -843,8 +844,8 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
   OutBuf b;
   if (!rc) rc = out_prepare(out, host, (size_t)n_freq * v.n_q, &b);
   if (rc) {
-    cudaFree(dg);
-    cudaFree(dq);
+    dev_free(dg, v.s);
+    dev_free(dq, v.s);
     return rc;
   }
   const unsigned nb = (unsigned)((v.n_q + QT - 1) / QT);
@@ -871,9 +872,8 @@ extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_fre
   cudaError_t e = cudaGetLastError();
   rc = e == cudaSuccess ? out_finish(out, host, (size_t)n_freq * v.n_q, &b, v.s)
                         : fail(MPSQ_ERR_CUDA, "gauss launch: %s", cudaGetErrorString(e));
-  cudaStreamSynchronize(v.s);
-  cudaFree(dg);
-  cudaFree(dq);
+  dev_free(dg, v.s);
+  dev_free(dq, v.s);
   return rc;
 }
 

@@ -257,6 +257,9 @@ class SqomJob:
         self._h = C.c_void_p()
         self._stream = int(stream or 0)
         self._copy_stream = None
+        self._d2h_stream = None      # output copies to host torch tensors
+        self._d2h_done = None
+        self._stage = {}             # device staging buffers of those outputs
         check(L.mpsq_job_create(C.byref(d), C.c_void_p(stream or 0), C.byref(self._h)), "job_create")
 
     # ------------------------------------------------------------------ lifecycle
@@ -308,12 +311,13 @@ class SqomJob:
         self.sync()
 
     # ------------------------------------------------------------------ compute
-    def transform_from_host(self, frames, chunk: int = 32):
+    def transform_from_host(self, frames, chunk: int = 32, first_chunk: int = 4):
         """Uploads host frames (count = n_frames; a pinned torch CPU tensor copies by DMA) in
-        chunks of `chunk` frames on a second CUDA stream and transforms every chunk on the
-        job's stream as soon as it has arrived, so the upload of chunk c+1 overlaps the
-        transform of chunk c.  Uploads start after all work already queued on the job's
-        stream, which may still read the previous trajectory."""
+        chunks of `chunk` frames (the first one `first_chunk` frames, to start computing
+        early) on a second CUDA stream and transforms every chunk on the job's stream as soon
+        as it has arrived, so the upload of chunk c+1 overlaps the transform of chunk c.
+        Uploads start after all work already queued on the job's stream, which may still read
+        the previous trajectory."""
         import torch
         if hasattr(frames, "is_cuda"):
             if frames.is_cuda:
@@ -337,8 +341,9 @@ class SqomJob:
         tail.record(job_stream)
         cs.wait_event(tail)
         frame_bytes = self.n_atoms_frame * 16
-        for c0 in range(0, F, chunk):
-            n = min(chunk, F - c0)
+        bounds = [0] + list(range(min(max(1, first_chunk), F), F, chunk)) + [F]
+        for c0, c1 in zip(bounds[:-1], bounds[1:]):
+            n = c1 - c0
             check(L.mpsq_job_set_frames_on(self._h, C.c_void_p(base + c0 * frame_bytes), c0, n, 1,
                                            C.c_void_p(cs.cuda_stream)), "set_frames_on")
             ev = torch.cuda.Event()
@@ -367,6 +372,49 @@ class SqomJob:
 
     def sync(self):
         check(_lib.load().mpsq_job_sync(self._h), "sync")
+        if self._d2h_stream is not None:
+            self._d2h_stream.synchronize()
+
+    def _torch_stream(self):
+        import torch
+        return torch.cuda.ExternalStream(self._stream) if self._stream else torch.cuda.default_stream()
+
+    def _target(self, out, key, shape):
+        """Where an output is computed: (pointer, host flag for the C call, host torch tensor
+        to copy to afterwards or None).  A host torch tensor (pinned for a real overlap) is
+        filled from a device staging buffer by an asynchronous copy on a separate stream, so
+        that the copy overlaps whatever the job's stream runs next; sync() or wait_outputs()
+        orders it."""
+        if out is None or not hasattr(out, "is_cuda"):
+            return out, 1, None
+        if out.is_cuda:
+            return out, 0, None
+        import torch
+        dev = self._stage.get(key)
+        if dev is None or tuple(dev.shape) != tuple(shape):
+            dev = torch.empty(shape, dtype=torch.float32, device="cuda")
+            self._stage[key] = dev
+        if self._d2h_done is not None:          # the previous copy out of the buffer
+            self._torch_stream().wait_event(self._d2h_done)
+        return dev, 0, out
+
+    def _copy_out(self, dev, host):
+        import torch
+        if self._d2h_stream is None:
+            self._d2h_stream = torch.cuda.Stream()
+        ready = torch.cuda.Event()
+        ready.record(self._torch_stream())
+        self._d2h_stream.wait_event(ready)
+        with torch.cuda.stream(self._d2h_stream):
+            host.copy_(dev.view(host.shape), non_blocking=True)
+        self._d2h_done = torch.cuda.Event()
+        self._d2h_done.record(self._d2h_stream)
+
+    def wait_outputs(self):
+        """Makes the job's stream wait, on the device, for the pending copies of outputs to
+        host tensors (no host synchronisation)."""
+        if self._d2h_done is not None:
+            self._torch_stream().wait_event(self._d2h_done)
 
     def profile(self, enable: bool = True):
         check(_lib.load().mpsq_job_profile(self._h, int(enable)), "profile")
@@ -419,13 +467,18 @@ class SqomJob:
         """Total S(Q) = <|cs|^2>_t / (sum N_j)^2 (:1381-1387, :1573-1574); s_trig > 0 applies
         the speckle filter before the (sum N)^2 norm (:1531-1570, plane grids)."""
         n2 = self.norm2() if normalize else 1.0
-        host = out is None or not hasattr(out, "is_cuda")
-        res = np.empty(self.grid.n_modes, f32) if out is None else out
+        res, host, copy_to = self._target(out, "sq", (self.grid.n_modes,))
+        if res is None:
+            res = np.empty(self.grid.n_modes, f32)
         if s_trig > 0:
             self._plane_shape("speckle filter")
             check(_lib.load().mpsq_job_sq_total(self._h, 1.0, C.c_void_p(ptr(res)), int(host)), "sq_total")
-            return self._speckle(res, s_trig, False, 1.0 / n2, host)
-        check(_lib.load().mpsq_job_sq_total(self._h, n2, C.c_void_p(ptr(res)), int(host)), "sq_total")
+            res = self._speckle(res, s_trig, False, 1.0 / n2, host)
+        else:
+            check(_lib.load().mpsq_job_sq_total(self._h, n2, C.c_void_p(ptr(res)), int(host)), "sq_total")
+        if copy_to is not None:
+            self._copy_out(res, copy_to)
+            return copy_to
         return res
 
     def _plane_shape(self, what):
@@ -533,10 +586,14 @@ class SqomJob:
         if normalize:
             scale *= t_step / self.norm2()
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
-        host = out is None or not hasattr(out, "is_cuda")
-        res = np.empty((n_freq, self.grid.n_modes), f32) if out is None else out
+        res, host, copy_to = self._target(out, "sqw", (n_freq, self.grid.n_modes))
+        if res is None:
+            res = np.empty((n_freq, self.grid.n_modes), f32)
         check(_lib.load().mpsq_job_sqw_gauss(self._h, float(fwhm), n_freq, C.c_void_p(ptr(q2)),
                                              scale, C.c_void_p(ptr(res)), int(host)), "sqw_gauss")
+        if copy_to is not None:
+            self._copy_out(res, copy_to)
+            return copy_to
         return res
 
 
