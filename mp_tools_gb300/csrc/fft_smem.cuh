@@ -1,6 +1,6 @@
 // Shared-memory FFT building blocks for the pruned fine-grid transform and the time-axis
 // spectrum: forward DFTs of lines of length n = 2^a 3^b 5^c held in shared memory, computed in
-// place by mixed-radix decimation in frequency (radix 8, 6, 4, 2, 3, 5 butterflies) with a
+// place by mixed-radix decimation in frequency (radix 24, 16, 12, 8, 6, 4, 2, 3, 5) with a
 // twiddle table tw[k] = exp(-2 pi i k / n); outputs are read at digit-reversed positions.
 #pragma once
 
@@ -107,40 +107,169 @@ __device__ __forceinline__ void dft6(float2* v) {
   v[5] = make_float2(e[2].x - t2.x, e[2].y - t2.y);
 }
 
+// Forward 16-point DFT in place, 4 x 4 Cooley-Tukey: for n = 4 n1 + n2 and k = k1 + 4 k2,
+// X[k] = sum_n2 W4^(n2 k2) [W16^(n2 k1) sum_n1 x[4 n1 + n2] W4^(n1 k1)].
+__device__ __forceinline__ float2 cmulc(float2 a, float c, float s) {  // a (c + i s)
+  return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+__device__ __forceinline__ void dft16(float2* v) {
+  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;  // cos, sin pi/8
+  const float r = 0.70710678118654752440f;
+  float2 y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    float2 a[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+    butterfly(a, 4);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = a[k1];
+  }
+  // W16^m = exp(-2 pi i m/16) for m = n2 k1: 1, 2, 3 | 2, 4, 6 | 3, 6, 9
+  y[1][1] = cmulc(y[1][1], c1, -s1);
+  y[1][2] = cmulc(y[1][2], r, -r);
+  y[1][3] = cmulc(y[1][3], s1, -c1);
+  y[2][1] = cmulc(y[2][1], r, -r);
+  y[2][2] = make_float2(y[2][2].y, -y[2][2].x);  // -i
+  y[2][3] = cmulc(y[2][3], -r, -r);
+  y[3][1] = cmulc(y[3][1], s1, -c1);
+  y[3][2] = cmulc(y[3][2], -r, -r);
+  y[3][3] = cmulc(y[3][3], -c1, s1);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 b[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    butterfly(b, 4);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+
+// Forward 12-point DFT in place, 4 x 3: n = 3 n1 + n2, k = k1 + 4 k2,
+// X[k] = sum_n2 W3^(n2 k2) [W12^(n2 k1) sum_n1 x[3 n1 + n2] W4^(n1 k1)].
+__device__ __forceinline__ void dft12(float2* v) {
+  const float h = 0.5f, s3 = 0.86602540378443864676f;
+  float2 y[3][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 3; ++n2) {
+    float2 a[4] = {v[n2], v[3 + n2], v[6 + n2], v[9 + n2]};
+    butterfly(a, 4);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = a[k1];
+  }
+  // W12^m for m = n2 k1: 1, 2, 3 | 2, 4, 6
+  y[1][1] = cmulc(y[1][1], s3, -h);
+  y[1][2] = cmulc(y[1][2], h, -s3);
+  y[1][3] = make_float2(y[1][3].y, -y[1][3].x);  // -i
+  y[2][1] = cmulc(y[2][1], h, -s3);
+  y[2][2] = cmulc(y[2][2], -h, -s3);
+  y[2][3] = make_float2(-y[2][3].x, -y[2][3].y);  // -1
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 b[3] = {y[0][k1], y[1][k1], y[2][k1]};
+    butterfly(b, 3);
+#pragma unroll
+    for (int k2 = 0; k2 < 3; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+
+// Forward 24-point DFT in place, 8 x 3: n = 3 n1 + n2, k = k1 + 8 k2,
+// X[k] = sum_n2 W3^(n2 k2) [W24^(n2 k1) sum_n1 x[3 n1 + n2] W8^(n1 k1)].
+__device__ __forceinline__ void dft24(float2* v) {
+  // cos and sin of 2 pi m / 24, m = 0..14
+  const float cs[15][2] = {
+      {1.0f, 0.0f},
+      {0.96592582628906828675f, 0.25881904510252076235f},
+      {0.86602540378443864676f, 0.5f},
+      {0.70710678118654752440f, 0.70710678118654752440f},
+      {0.5f, 0.86602540378443864676f},
+      {0.25881904510252076235f, 0.96592582628906828675f},
+      {0.0f, 1.0f},
+      {-0.25881904510252076235f, 0.96592582628906828675f},
+      {-0.5f, 0.86602540378443864676f},
+      {-0.70710678118654752440f, 0.70710678118654752440f},
+      {-0.86602540378443864676f, 0.5f},
+      {-0.96592582628906828675f, 0.25881904510252076235f},
+      {-1.0f, 0.0f},
+      {-0.96592582628906828675f, -0.25881904510252076235f},
+      {-0.86602540378443864676f, -0.5f}};
+  float2 y[3][8];
+#pragma unroll
+  for (int n2 = 0; n2 < 3; ++n2) {
+    float2 a[8];
+#pragma unroll
+    for (int n1 = 0; n1 < 8; ++n1) a[n1] = v[3 * n1 + n2];
+    dft8(a);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) y[n2][k1] = a[k1];
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < 3; ++n2)
+#pragma unroll
+    for (int k1 = 1; k1 < 8; ++k1) {
+      const int m = n2 * k1;                              // W24^m = cos - i sin
+      y[n2][k1] = cmulc(y[n2][k1], cs[m][0], -cs[m][1]);
+    }
+#pragma unroll
+  for (int k1 = 0; k1 < 8; ++k1) {
+    float2 b[3] = {y[0][k1], y[1][k1], y[2][k1]};
+    butterfly(b, 3);
+#pragma unroll
+    for (int k2 = 0; k2 < 3; ++k2) v[k1 + 8 * k2] = b[k2];
+  }
+}
+
 // Radices of an in-place decimation-in-frequency transform of length N = 2^a 3^b 5^c, in
-// application order: 8 while 8 divides what remains, then 6, 4, 2, 3 or 5.
-__host__ __device__ constexpr int dif_next(int rem) {
+// application order.  Two stages when N = r0 r1 with r0 in {16, 24, 12, 8} and r1 in
+// {24, 16, 12, 8, 6} (fewer passes through shared memory); otherwise 8 while 8 divides what
+// remains, then 6, 4, 2, 3 or 5.
+__host__ __device__ constexpr bool dif_final(int r) {
+  return r == 24 || r == 16 || r == 12 || r == 8 || r == 6;
+}
+__host__ __device__ constexpr int dif_first(int N) {
+  return (N % 16 == 0 && dif_final(N / 16)) ? 16
+         : (N % 24 == 0 && dif_final(N / 24)) ? 24
+         : (N % 12 == 0 && dif_final(N / 12)) ? 12
+         : (N % 8 == 0 && dif_final(N / 8)) ? 8
+                                             : 0;
+}
+__host__ __device__ constexpr int dif_greedy(int rem) {
   return rem % 8 == 0 ? 8 : rem % 6 == 0 ? 6 : rem % 4 == 0 ? 4 : rem % 2 == 0 ? 2 : rem % 3 == 0 ? 3 : 5;
 }
-__host__ __device__ constexpr int dif_radix(int N, int s) {
+// P selects the plan: kDifTwoStage (the two-stage split where one exists) or kDifGreedy
+// (radix 8 first: smaller register footprint for kernels that hold more state).
+constexpr int kDifGreedy = 0, kDifTwoStage = 1;
+__host__ __device__ constexpr int dif_radix(int N, int s, int P = kDifTwoStage) {
+  if (P == kDifTwoStage && dif_first(N)) return s == 0 ? dif_first(N) : N / dif_first(N);
   int rem = N;
-  for (int i = 0; i < s; ++i) rem /= dif_next(rem);
-  return dif_next(rem);
+  for (int i = 0; i < s; ++i) rem /= dif_greedy(rem);
+  return dif_greedy(rem);
 }
-__host__ __device__ constexpr int dif_stages(int N) {
+__host__ __device__ constexpr int dif_stages(int N, int P = kDifTwoStage) {
+  if (P == kDifTwoStage && dif_first(N)) return 2;
   int s = 0;
-  for (int rem = N; rem > 1; rem /= dif_next(rem)) ++s;
+  for (int rem = N; rem > 1; rem /= dif_greedy(rem)) ++s;
   return s;
 }
-__host__ __device__ constexpr int dif_block(int N, int s) {
+__host__ __device__ constexpr int dif_block(int N, int s, int P = kDifTwoStage) {
   int b = N;
-  for (int i = 0; i < s; ++i) b /= dif_radix(N, i);
+  for (int i = 0; i < s; ++i) b /= dif_radix(N, i, P);
   return b;
 }
 __device__ __forceinline__ void dft_r(float2* v, int r) {
-  if (r == 8) dft8(v);
+  if (r == 24) dft24(v);
+  else if (r == 16) dft16(v);
+  else if (r == 12) dft12(v);
+  else if (r == 8) dft8(v);
   else if (r == 6) dft6(v);
   else butterfly(v, r);
 }
 
 // Position of frequency f in the output of the in-place DIF transform (mixed-radix digit
 // reversal: stage s leaves digit k'_s of f = k'_0 + r_0 (k'_1 + r_1 (...)) at stride M_s).
-template <int N>
+template <int N, int P = kDifTwoStage>
 __device__ __forceinline__ int dif_position(int f) {
   int p = 0, block = N;
 #pragma unroll
-  for (int s = 0; s < dif_stages(N); ++s) {
-    const int r = dif_radix(N, s);
+  for (int s = 0; s < dif_stages(N, P); ++s) {
+    const int r = dif_radix(N, s, P);
     block /= r;
     p += (f % r) * block;
     f /= r;
@@ -160,13 +289,34 @@ struct DifNoPre {
   __device__ __forceinline__ void operator()(float2 (&)[R], int, int, int) const {}
 };
 
-template <int N, int L, int S, class Pre>
+template <int N, int L, int S, int P, class Pre>
 __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
                                                const float2* __restrict__ tw, const Pre& pre) {
-  if constexpr (S < dif_stages(N)) {
-    constexpr int r = dif_radix(N, S);
-    constexpr int B = dif_block(N, S);
+  if constexpr (S < dif_stages(N, P)) {
+    constexpr int r = dif_radix(N, S, P);
+    constexpr int B = dif_block(N, S, P);
     constexpr int M = B / r;
+    if constexpr (r > 8) {
+      // large radix: one line per thread (register budget), 8-byte accesses
+      for (int e = threadIdx.x; e < L * (N / r); e += blockDim.x) {
+        const int ln = e % L, gi = e / L;
+        const int j = gi % M, base = (gi / M) * B + j;
+        float2 va[r];
+#pragma unroll
+        for (int k = 0; k < r; ++k) va[k] = xs[(base + M * k) * L + ln];
+        if constexpr (S == 0) pre(va, base, M, ln);
+        dft_r(va, r);
+        if constexpr (M > 1) {
+#pragma unroll
+          for (int k = 1; k < r; ++k) va[k] = cmulf(va[k], tw[(N / B) * j * k]);
+        }
+#pragma unroll
+        for (int k = 0; k < r; ++k) xs[(base + M * k) * L + ln] = va[k];
+      }
+      __syncthreads();
+      dif_lines_from<N, L, S + 1, P>(xs, tw, pre);
+      return;
+    }
     constexpr int LP = L / 2;      // a thread transforms two adjacent lines (16-byte accesses)
     for (int e = threadIdx.x; e < LP * (N / r); e += blockDim.x) {
       const int lp = e % LP, gi = e / LP;
@@ -198,15 +348,15 @@ __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
             make_float4(va[k].x, va[k].y, vb[k].x, vb[k].y);
     }
     __syncthreads();
-    dif_lines_from<N, L, S + 1>(xs, tw, pre);
+    dif_lines_from<N, L, S + 1, P>(xs, tw, pre);
   }
 }
 // L must be even; xs must be 16-byte aligned.
-template <int N, int L, class Pre = DifNoPre>
+template <int N, int L, class Pre = DifNoPre, int P = kDifTwoStage>
 __device__ __forceinline__ void dif_lines(float2* __restrict__ xs, const float2* __restrict__ tw,
                                           const Pre& pre = Pre()) {
   static_assert(L % 2 == 0, "dif_lines transforms lines in pairs");
-  dif_lines_from<N, L, 0>(xs, tw, pre);
+  dif_lines_from<N, L, 0, P>(xs, tw, pre);
 }
 
 // tw[n] = exp(-2 pi i n / N), n < N (all threads of the block; no barrier).

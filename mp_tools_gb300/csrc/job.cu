@@ -525,7 +525,7 @@ __device__ __forceinline__ int wrap_freq(int f, int n) { return f < 0 ? f + n : 
 // pairs of the tile; the K0 kept frequencies of each row pair are gathered into registers,
 // staged as [row][K0] and stored as one contiguous block.
 template <int N>
-__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
+__global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     fftx_dif_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
                     const float2* __restrict__ gtw, int h0, int K0, float2* __restrict__ b1) {
   constexpr int L = kPassLines, LP = L / 2, NP = N / 2;
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
 // Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA; a thread moves
 // two adjacent columns.
 template <int N>
-__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
+__global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     ffty_dif_kernel(const float2* __restrict__ b1, int n2, int K0, const float2* __restrict__ gtw,
                     int h1, int K1, float2* __restrict__ b2) {
   constexpr int L = kPassLines, LP = L / 2;
@@ -641,7 +641,7 @@ template <int N>
 __host__ __device__ constexpr int zpass_cols() { return 8; }
 
 template <int N>
-__global__ void __launch_bounds__(256, (N <= 512 ? 4 : 1))
+__global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     fftz_dif_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
                            int h0, int h1, int h2, int ngroups, const float2* __restrict__ gtw,
                            const float* __restrict__ c0, const float* __restrict__ c1,
