@@ -116,6 +116,11 @@ struct mpsq_job {
   void* fine = nullptr;
   int* counts = nullptr;
   int* starts = nullptr;
+  // locality order of the atoms (rebuilt from the first frame of each multi-frame transform)
+  int* perm = nullptr;
+  int* perm_counts = nullptr;
+  int* perm_starts = nullptr;
+  bool perm_built = false;
   void* recs = nullptr;
   void* str = nullptr;
   int64_t cap = 0;
@@ -154,43 +159,55 @@ struct mpsq_job {
 
 namespace mpsq {
 
-// Selection, phases and strengths of one atom of one frame (mp_sqom56.f90:1104-1142), then
-// binning.  Pass 0 (kScatter false) counts, pass 1 scatters; str == nullptr: unit strengths
-// (no centre phase, no window), which are not stored.
-template <typename T, bool kScatter>
-__global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
-                               PrepArgs p, SpreadArgs a, int* cursor,
-                               const int* __restrict__ starts, typename RecOf<T>::type* recs,
-                               typename Cplx<T>::type* str, int64_t cap, int* err) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= p.n_atoms_frame) return;
+// Selection, phases and strengths of one atom of one frame (mp_sqom56.f90:1104-1142): false
+// for an atom that is not transformed; otherwise its grid, pair component and strength and
+// either its first support cell and offset (FP32 split path) or its folded fine-grid
+// coordinate (FP64 and phase-rounding paths).
+template <typename T>
+struct PointPrep {
+  int grid, comp;
+  bool split;
+  int sc[3];
+  float dc[3];
+  double g[3];
+  typename Cplx<T>::type c;
+};
+
+template <typename T>
+__device__ __forceinline__ bool prep_point(const float4* __restrict__ frame,
+                                           const int4* __restrict__ at_ind, const PrepArgs& p,
+                                           const SpreadArgs& a, int64_t j, PointPrep<T>& o) {
   int s = 0;
   while (s + 1 < p.n_species && j >= p.species_offset[s + 1]) ++s;
-  if (j < p.species_offset[0] || j >= p.species_offset[p.n_species]) return;
+  if (j < p.species_offset[0] || j >= p.species_offset[p.n_species]) return false;
   const int grid = p.group_of[s];
-  if (grid < 0) return;
+  if (grid < 0) return false;
   const float4 r = frame[j];
   if (p.input_method == MPSQ_CELL) {
-    if (r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) return;  // vacancy (:1107)
+    if (r.x == 0.0f && r.y == 0.0f && r.z == 0.0f) return false;  // vacancy (:1107)
     if (p.use_range && at_ind) {
       const int4 ci = at_ind[j];
       const int c3[3] = {ci.x, ci.y, ci.z};
       for (int k = 0; k < 3; ++k) {
         const int c = c3[k] - p.n_row[k] / 2 - 1;
-        if ((float)c < p.pos_min_f[k] || (float)c > p.pos_max_f[k]) return;  // (:1109-1111)
+        if ((float)c < p.pos_min_f[k] || (float)c > p.pos_max_f[k]) return false;  // (:1109-1111)
       }
     }
   } else {
     const float rr[3] = {r.x, r.y, r.z};
     for (int k = 0; k < 3; ++k)  // (:1121-1128)
-      if (!(rr[k] >= p.pos_min_f[k] - p.tol_f && rr[k] < p.pos_max_f[k] + p.tol_f)) return;
+      if (!(rr[k] >= p.pos_min_f[k] - p.tol_f && rr[k] < p.pos_max_f[k] + p.tol_f)) return false;
   }
   if constexpr (sizeof(T) == 4) {
     if (!p.phase_rounding) {
       // FP32 split precision: exact phase reduction in two-float arithmetic (no FP64 pipe)
       const float rf[3] = {r.x, r.y, r.z};
-      int sc[3] = {0, 0, 0};
-      float dc[3] = {0.0f, 0.0f, 0.0f};
+      int* const sc = o.sc;
+      float* const dc = o.dc;
+      for (int k = 0; k < 3; ++k) {
+        sc[k] = 0;
+        dc[k] = 0.0f;
+      }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {  // unrolled: sc, dc stay in registers
         if (k < p.dim) {
@@ -218,11 +235,13 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
         c.x *= f;
         c.y *= f;
       }
-      const int comp = p.pack ? p.comp_of[s] : 0;
-      if (p.pack && c.x == 0.0f) return;
-      emit_cells<float>(a, sc, dc, grid, comp, kScatter, cursor, starts, (RecF*)recs,
-                        (float2*)str, c, nullptr, 0, cap, err);
-      return;
+      o.comp = p.pack ? p.comp_of[s] : 0;
+      if (p.pack && c.x == 0.0f) return false;
+      o.grid = grid;
+      o.split = true;
+      o.c.x = (T)c.x;
+      o.c.y = (T)c.y;
+      return true;
     }
   }
   double x[3] = {0.0, 0.0, 0.0};
@@ -287,10 +306,72 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
     c.x *= f;
     c.y *= f;
   }
-  const int comp = p.pack ? p.comp_of[s] : 0;
-  if (p.pack && c.x == (T)0) return;  // zero strength contributes nothing
-  emit_records<T>(a, g, grid, comp, kScatter, cursor, starts, recs, str, c, nullptr, 0, cap,
-                  err);
+  o.comp = p.pack ? p.comp_of[s] : 0;
+  if (p.pack && c.x == (T)0) return false;  // zero strength contributes nothing
+  o.grid = grid;
+  o.split = false;
+  o.c = c;
+  for (int k = 0; k < 3; ++k) o.g[k] = g[k];
+  return true;
+}
+
+// Binning of one frame.  Pass 0 (kScatter false) counts, pass 1 scatters; str == nullptr:
+// unit strengths (no centre phase, no window), which are not stored.  Thread i takes atom
+// perm[i] (a locality order, so that a warp's atoms share tiles and its cursor atomics
+// combine) or atom i without a permutation.
+template <typename T, bool kScatter>
+__global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
+                               const int* __restrict__ perm, PrepArgs p, SpreadArgs a,
+                               int* cursor, const int* __restrict__ starts,
+                               typename RecOf<T>::type* recs, typename Cplx<T>::type* str,
+                               int64_t cap, int* err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n_atoms_frame) return;
+  const int64_t j = perm ? perm[i] : i;
+  PointPrep<T> q;
+  if (!prep_point<T>(frame, at_ind, p, a, j, q)) return;
+  if constexpr (sizeof(T) == 4) {
+    if (q.split) {
+      const float2 c = make_float2(q.c.x, q.c.y);
+      emit_cells<float>(a, q.sc, q.dc, q.grid, q.comp, kScatter, cursor, starts, (RecF*)recs,
+                        (float2*)str, c, nullptr, 0, cap, err);
+      return;
+    }
+  }
+  emit_records<T>(a, q.g, q.grid, q.comp, kScatter, cursor, starts, recs, str, q.c, nullptr, 0,
+                  cap, err);
+}
+
+// Locality order of the atoms of one frame: a counting sort by the tile of each atom's first
+// support cell (atoms that are not transformed go to a last bucket, key nkeys).  Pass 0
+// counts, pass 1 writes perm[starts[key] + slot] = atom.
+template <typename T, bool kScatter>
+__global__ void job_perm_kernel(const float4* __restrict__ frame, const int4* __restrict__ at_ind,
+                                PrepArgs p, SpreadArgs a, int64_t nkeys, int* cursor,
+                                const int* __restrict__ starts, int* __restrict__ perm) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.n_atoms_frame) return;
+  PointPrep<T> q;
+  int64_t key = nkeys;
+  if (prep_point<T>(frame, at_ind, p, a, j, q)) {
+    int t[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        const int c = q.split ? q.sc[k] : (int)ceil(q.g[k] - 0.5 * a.w);
+        int tk = c >> a.tshift[k];
+        tk = tk < 0 ? tk + a.ntile[k] : (tk >= a.ntile[k] ? tk - a.ntile[k] : tk);
+        t[k] = tk;
+      }
+    }
+    key = (int64_t)q.grid * a.n_tiles + ((int64_t)t[2] * a.ntile[1] + t[1]) * a.ntile[0] + t[0];
+  }
+  if constexpr (!kScatter) {
+    atomicAdd(&cursor[key], 1);
+  } else {
+    const int slot = atomicAdd(&cursor[key], 1);
+    perm[starts[key] + slot] = (int)j;
+  }
 }
 
 template <typename T>
@@ -895,6 +976,9 @@ static void job_free(mpsq_job* j) {
   cudaFree(j->fine);
   cudaFree(j->counts);
   cudaFree(j->starts);
+  cudaFree(j->perm);
+  cudaFree(j->perm_counts);
+  cudaFree(j->perm_starts);
   cudaFree(j->recs);
   cudaFree(j->str);
   for (int a = 0; a < 3; ++a) cudaFree(j->corr[a]);
@@ -934,6 +1018,7 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
   b += (int64_t)std::max(1, ng) * g.n_fine * (int64_t)csize(d->precision);  // fine grids
   b += d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision));
   b += (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8;
+  b += d->n_atoms_frame * 4 + (int64_t)(std::max(1, ng) * g.n_tiles + 2) * 8;  // locality order
   b += (int64_t)d->n_frames * g.n_modes * (int64_t)csize(d->precision);     // cs(t,Q)
   if (d->store_species)
     b += (int64_t)d->n_frames * d->n_species * g.n_modes * (int64_t)csize(d->precision);
@@ -1082,6 +1167,9 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   A(&j->fine, (size_t)a.ngrid * j->g.n_fine * cs);
   A((void**)&j->counts, sizeof(int) * (nkeys + 1));
   A((void**)&j->starts, sizeof(int) * (nkeys + 1));
+  A((void**)&j->perm, sizeof(int) * std::max<int64_t>(d->n_atoms_frame, 1));
+  A((void**)&j->perm_counts, sizeof(int) * (nkeys + 2));
+  A((void**)&j->perm_starts, sizeof(int) * (nkeys + 2));
   A(&j->recs, (size_t)j->cap * rsize(prec));
   A(&j->str, (size_t)j->cap * cs);
   A(&j->cs, (size_t)d->n_frames * j->g.n_modes * cs);
@@ -1232,6 +1320,23 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
   // job's stream waits for the second lane at the end
   const bool two = j->lane2 && !prof && count > 1;
   cudaStream_t const main_s = j->s;
+  // locality order from the first frame (atoms move little between frames; any order gives the
+  // same records, a spatial one lets a warp's cursor atomics combine)
+  if (count > 1 && j->ngroups > 0) {
+    const float4* f0 = j->traj + (size_t)first * j->d.n_atoms_frame;
+    MPSQ_CUDA_TRY(cudaMemsetAsync(j->perm_counts, 0, sizeof(int) * (nkeys + 2), main_s));
+    job_perm_kernel<T, false><<<nb, bt, 0, main_s>>>(f0, j->at_ind, j->pa, a, nkeys,
+                                                      j->perm_counts, j->perm_starts, j->perm);
+    MPSQ_LAUNCH_CHECK();
+    int rc = launch_scan<T>(j->perm_counts, j->perm_starts, nkeys + 1, main_s);
+    if (rc) return rc;
+    MPSQ_CUDA_TRY(cudaMemsetAsync(j->perm_counts, 0, sizeof(int) * (nkeys + 2), main_s));
+    job_perm_kernel<T, true><<<nb, bt, 0, main_s>>>(f0, j->at_ind, j->pa, a, nkeys,
+                                                     j->perm_counts, j->perm_starts, j->perm);
+    MPSQ_LAUNCH_CHECK();
+    j->perm_built = true;
+  }
+  const int* const perm = j->perm_built ? j->perm : nullptr;
   // unit strengths (no centre phase, no spatial window) are implied, not stored
   const bool unit_str = !j->pa.has_qc && !j->pa.window;
   if (two) {
@@ -1251,7 +1356,7 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     if (mark(0)) return MPSQ_ERR_CUDA;
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, counts, starts,
+      job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, starts,
                                                  (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
@@ -1259,7 +1364,7 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
     if (rc) return rc;
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T, true><<<nb, bt, 0, s>>>(frame, j->at_ind, j->pa, a, counts, starts,
+      job_bin_kernel<T, true><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, starts,
                                                 (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }

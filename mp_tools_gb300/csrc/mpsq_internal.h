@@ -203,7 +203,8 @@ __device__ __forceinline__ void split_cell_f2(F2 g, int nf, float inv_nf, int w,
 // Pass 0 (scatter = false) counts records per (grid, tile) key into `cursor`; pass 1 writes
 // them at starts[key] + slot, `cursor` having been zeroed between the passes.  The up to 8
 // candidate tiles are handled in phases (keys, then all cursor atomics, then all stores) so
-// that the atomics' round trips overlap instead of following one another.
+// that the atomics' round trips overlap instead of following one another.  Every lane that
+// is still running in the warp must call it (the atomics are combined across the warp).
 template <typename T>
 __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3], const T d_in[3],
                                            int keygrid, int comp, bool scatter, int* cursor,
@@ -232,7 +233,7 @@ __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3
     }
   }
   const int64_t gbase = (int64_t)keygrid * a.n_tiles;
-  int64_t key[8];
+  int key[8];   // < ngrid * n_tiles < 2^31
   int slot[8];
   int packed[8];
 #pragma unroll
@@ -245,21 +246,37 @@ __device__ __forceinline__ void emit_cells(const SpreadArgs& a, const int s_in[3
     const int lx = loc_lo[0] - (ix << a.tshift[0]);
     const int ly = loc_lo[1] - (iy << a.tshift[1]);
     const int lz = loc_lo[2] - (iz << a.tshift[2]);
-    key[c] = gbase + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx;
+    key[c] = (int)(gbase + ((int64_t)wz * a.ntile[1] + wy) * a.ntile[0] + wx);
     packed[c] = (lx + 64) | ((ly + 64) << 8) | ((lz + 64) << 16) | (comp << 24);
   }
+  // Cursor atomics combined per warp: the lanes that share a key take consecutive slots from
+  // one atomic of their lowest lane (points in locality order share most keys).
+  const unsigned live = __activemask();
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int ix = c & 1, iy = (c >> 1) & 1, iz = c >> 2;
-    if ((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2])) continue;
-    slot[c] = atomicAdd(&cursor[key[c]], 1);
+    const bool has = !((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2]));
+    const unsigned act = __ballot_sync(live, has);
+    if (has) {
+      const unsigned peers = __match_any_sync(act, key[c]);
+      const int leader = __ffs(peers) - 1;
+      if (!scatter) {
+        if (lane == leader) atomicAdd(&cursor[key[c]], __popc(peers));
+      } else {
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[key[c]], __popc(peers));
+        slot[c] = __shfl_sync(peers, base, leader) + __popc(peers & below);
+      }
+    }
   }
   if (!scatter) return;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int ix = c & 1, iy = (c >> 1) & 1, iz = c >> 2;
     if ((ix && !two[0]) || (iy && !two[1]) || (iz && !two[2])) continue;
-    const int64_t pos = (int64_t)starts[key[c]] + slot[c];
+    const int64_t pos = (int64_t)starts[key[c]] + slot[c];   // key + 1 <= ngrid * n_tiles
     if (pos >= (int64_t)starts[key[c] + 1] || pos >= cap) {
       atomicOr(err, 1);
       continue;
