@@ -51,6 +51,7 @@ struct PrepArgs {
   float qhi[3], qlo[3];
   float inv_nf[3];
   int nf[3];
+  int diag;   // 1: A is diagonal (axis-aligned grid), g_k needs only r_k
 };
 
 // Parameters of the fused deconvolution / weighting.
@@ -211,7 +212,9 @@ __device__ __forceinline__ bool prep_point(const float4* __restrict__ frame,
 #pragma unroll
       for (int k = 0; k < 3; ++k) {  // unrolled: sc, dc stay in registers
         if (k < p.dim) {
-          const F2 gk = affine_f2(rf, p.ahi[k], p.alo[k], p.bhi[k], p.blo[k]);
+          // (the zero off-diagonal terms of an axis-aligned grid add exactly nothing)
+          const F2 gk = p.diag ? affine1_f2(rf[k], p.ahi[k][k], p.alo[k][k], p.bhi[k], p.blo[k])
+                               : affine_f2(rf, p.ahi[k], p.alo[k], p.bhi[k], p.blo[k]);
           split_cell_f2(gk, p.nf[k], p.inv_nf[k], a.w, &sc[k], &dc[k]);
         }
       }
@@ -601,17 +604,19 @@ __device__ __forceinline__ void copy_twiddles(float2* tw, const float2* __restri
 }
 __device__ __forceinline__ int wrap_freq(int f, int n) { return f < 0 ? f + n : f; }
 
-// Pass X: 16 contiguous rows of length N per CTA (one grid per blockIdx.y).  A thread reads two
-// adjacent complex of two adjacent rows (16 bytes each) and stores them as two 16-byte row
-// pairs of the tile; the K0 kept frequencies of each row pair are gathered into registers,
-// staged as [row][K0] and stored as one contiguous block.
-template <int N>
-__global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
+// Pass X: L contiguous rows of length N per CTA of 16 L threads (one grid per blockIdx.y).  A
+// thread reads two adjacent complex of two adjacent rows (16 bytes each) and stores them as
+// two 16-byte row pairs of the tile; the K0 kept frequencies of each row pair are gathered
+// into registers, staged as [row][K0] and stored as one contiguous block.  Small CTAs (8 rows)
+// let more of them share an SM, so that the loads of some overlap the transforms of others.
+constexpr int kPassLinesX = 8;
+template <int N, int L>
+__global__ void __launch_bounds__(16 * L, (N <= 512 ? 48 / L : 1))
     fftx_dif_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
                     const float2* __restrict__ gtw, int h0, int K0, float2* __restrict__ b1) {
-  constexpr int L = kPassLines, LP = L / 2, NP = N / 2;
-  constexpr int LOADS = (LP * NP + 255) / 256;          // (row pair, x pair) items per thread
-  constexpr int OUTS = (LP * (N / 2 + 1) + 255) / 256;  // kept row-pair values (K0 <= N/2+1)
+  constexpr int NT = 16 * L, LP = L / 2, NP = N / 2;
+  constexpr int LOADS = (LP * NP + NT - 1) / NT;          // (row pair, x pair) items per thread
+  constexpr int OUTS = (LP * (N / 2 + 1) + NT - 1) / NT;  // kept row-pair values (K0 <= N/2+1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);    // [N][L], then [L][K0]
   float2* tw = xs + N * L;
@@ -623,7 +628,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   float4 va[LOADS], vb[LOADS];
 #pragma unroll
   for (int p = 0; p < LOADS; ++p) {
-    const int e = tid + 256 * p;
+    const int e = tid + NT * p;
     const int rp = e % LP, xp = e / LP;
     va[p] = vb[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (e < LP * NP) {
@@ -633,7 +638,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   }
 #pragma unroll
   for (int p = 0; p < LOADS; ++p) {
-    const int e = tid + 256 * p;
+    const int e = tid + NT * p;
     if (e < LP * NP) {
       const int rp = e % LP, x = 2 * (e / LP);
       *reinterpret_cast<float4*>(&xs[x * L + 2 * rp]) = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
@@ -645,7 +650,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   float4 o[OUTS];
 #pragma unroll
   for (int p = 0; p < OUTS; ++p) {
-    const int e = tid + 256 * p;
+    const int e = tid + NT * p;
     o[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (e < LP * K0)
       o[p] = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(e / LP - h0, N)) * L + 2 * (e % LP)]);
@@ -653,7 +658,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < OUTS; ++p) {
-    const int e = tid + 256 * p;
+    const int e = tid + NT * p;
     if (e < LP * K0) {
       const int r = 2 * (e % LP), i = e / LP;
       xs[r * K0 + i] = make_float2(o[p].x, o[p].y);
@@ -662,7 +667,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   }
   __syncthreads();
   float2* dst = b1 + ((int64_t)g * n_rows + row0) * K0;
-  for (int e = tid; e < rows * K0; e += 256) dst[e] = xs[e];
+  for (int e = tid; e < rows * K0; e += NT) dst[e] = xs[e];
 }
 
 // Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA; a thread moves
@@ -861,10 +866,11 @@ static size_t pass_smem(int lines) {
 template <int N>
 static int launch_prune_x(const PruneLaunch& p) {
   const int n_rows = p.n[1] * p.n[2];
-  const size_t sm = pass_smem<N>(kPassLines);
-  cudaFuncSetAttribute(fftx_dif_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  fftx_dif_kernel<N><<<dim3((unsigned)((n_rows + kPassLines - 1) / kPassLines), (unsigned)p.ngrid),
-                       256, sm, p.s>>>(p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
+  constexpr int L = kPassLinesX;
+  const size_t sm = pass_smem<N>(L);
+  cudaFuncSetAttribute(fftx_dif_kernel<N, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  fftx_dif_kernel<N, L><<<dim3((unsigned)((n_rows + L - 1) / L), (unsigned)p.ngrid), 16 * L, sm,
+                          p.s>>>(p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
@@ -1099,6 +1105,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   p.window = d->spatial_window;
   p.pack = pack;
   p.n_atoms_frame = d->n_atoms_frame;
+  p.diag = 1;
   for (int k = 0; k < 3; ++k) {
     const double sc = d->tpe[k] * a.gscale[k];  // radians -> fine-grid units along axis k
     double bk = 0.0;
@@ -1113,6 +1120,8 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
     p.qhi[k] = (float)d->q_center[k];
     p.qlo[k] = (float)(d->q_center[k] - (double)p.qhi[k]);
     p.nf[k] = (int)j->g.nf[k];
+    for (int b = 0; b < 3; ++b)
+      if (b != k && (p.ahi[k][b] != 0.0f || p.alo[k][b] != 0.0f)) p.diag = 0;
     p.inv_nf[k] = (float)(1.0 / (double)j->g.nf[k]);
   }
   // weighting parameters

@@ -156,6 +156,15 @@ __device__ __forceinline__ F2 affine_f2(const float r[3], const float* ahi, cons
   const F2 s = two_sum(hi, lo);
   return s;
 }
+// The same for one term: r (A_hi + A_lo) + (B_hi + B_lo), identical to affine_f2 with the
+// other two coefficients zero (for finite r).
+__device__ __forceinline__ F2 affine1_f2(float r, float ahi, float alo, float bhi, float blo) {
+  const float p = __fmul_rn(r, ahi);
+  const float pe = fmaf(r, ahi, -p);
+  const F2 s = two_sum(bhi, p);
+  const float lo = __fadd_rn(blo, __fadd_rn(s.lo, fmaf(r, alo, pe)));
+  return two_sum(s.hi, lo);
+}
 // Folds g = hi + lo into [0, nf) and returns the first support cell s = ceil(g - w/2) and the
 // offset d = s - g in [-w/2, -w/2 + 1), both exact up to the FP32 rounding of d.
 __device__ __forceinline__ void split_cell_f2(F2 g, int nf, float inv_nf, int w, int* s, float* d) {
