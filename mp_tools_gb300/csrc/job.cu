@@ -719,12 +719,45 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   }
 }
 
-// Pass Z fused with the deconvolution: CTA (x-tile, ky index iy) loads, for every grid, the T
-// z-columns (iy, x0..x0+T) and their mirrors (2h1-iy, 2h0-x), transforms all 2T lines, and
-// accumulates the weighted species amplitudes of its T x m2 output modes in registers (two
-// adjacent columns per thread).
+// Pass Z fused with the deconvolution: CTA (x-tile, ky index iy <= h1) loads, for every grid,
+// the T z-columns P = (iy, x0..x0+T) and their mirrors M = (2h1-iy, 2h0-x), transforms all 2T
+// lines and forms the weighted species amplitudes of both the P modes and the M modes: the
+// pair separation of a mode k reads G(k) and G(-k), and the lines of P and M hold exactly the
+// two for either (so every column is loaded and transformed once).  A row that is its own
+// mirror (iy = h1) takes only its P modes; rows beyond the output range are skipped.
 template <int N>
 __host__ __device__ constexpr int zpass_cols() { return 8; }
+
+// One output mode from its line value G = G(k) and the mirror value Gm = G(-k): pair
+// separation, deconvolution, species weights; returns the weighted amplitude (without the
+// window norm) and writes the per-species amplitudes when they are stored.
+__device__ __forceinline__ float2 zpass_mode(float2 G, float2 Gm, bool pair, int sa, int sb,
+                                             float corr, int kx, int ky, int kz,
+                                             const WeightArgs& w, int64_t q, int64_t nm,
+                                             float2* __restrict__ cs_species_frame) {
+  float s2 = 0.f;
+  if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+    float qv[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
+    s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
+  }
+  if (pair) {
+    const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
+    const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
+    const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
+    if (w.store_species) {
+      cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
+      cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
+    }
+    return make_float2(wa * ar + wb * br, wa * ai + wb * bi);
+  }
+  const float wa = species_weight<float>(w, sa, s2);
+  if (w.store_species)
+    cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
+  return make_float2(wa * G.x * corr, wa * G.y * corr);
+}
 
 template <int N>
 __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
@@ -742,16 +775,18 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * T, iy = blockIdx.y;
   const int iym = 2 * h1 - iy;
+  const bool mrow = iym < m1 && iym != iy;              // this CTA also forms the row iym
   const int64_t nm = (int64_t)m0 * m1 * m2;
   copy_twiddles<N>(tw, gtw);
-  float4 acc[OUTS];
+  float4 acc[OUTS], accm[OUTS];
 #pragma unroll
-  for (int p = 0; p < OUTS; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float cy = c1[iy];
-  const int ky = iy - h1;
+  for (int p = 0; p < OUTS; ++p) acc[p] = accm[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float cy = c1[iy], cym = mrow ? c1[iym] : 0.0f;
+  const int ky = iy - h1, kym = iym - h1;
   for (int g = 0; g < ngroups; ++g) {
     const float2* src = b2 + (int64_t)g * N * K1 * K0;
     const int pair = w.pair[g];
+    const bool need_m = pair || mrow;
     if (g > 0) __syncthreads();  // the previous group's reads of the tile are complete
     for (int b0 = 0; b0 < LOADS; b0 += BATCH) {
       float2 va[BATCH], vb[BATCH];
@@ -763,10 +798,10 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
         const int c = mirror ? l - T : l;
         const int x = x0 + c;
         va[p] = vb[p] = make_float2(0.f, 0.f);
-        if (b0 + p < LOADS && e < LP * N && (!mirror || pair)) {
+        if (b0 + p < LOADS && e < LP * N && (!mirror || need_m)) {
           const float2* row = src + ((int64_t)z * K1 + (mirror ? iym : iy)) * K0;
-          if (x < m0) va[p] = __ldcs(row + (mirror ? 2 * h0 - x : x));
-          if (x + 1 < m0) vb[p] = __ldcs(row + (mirror ? 2 * h0 - x - 1 : x + 1));
+          if (x < K0) va[p] = __ldcs(row + (mirror ? 2 * h0 - x : x));
+          if (x + 1 < K0) vb[p] = __ldcs(row + (mirror ? 2 * h0 - x - 1 : x + 1));
         }
       }
 #pragma unroll
@@ -783,53 +818,46 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     for (int p = 0; p < OUTS; ++p) {
       const int e = tid + 256 * p;
       const int c = 2 * (e % TP), iz = e / TP;
-      if (iz >= m2 || x0 + c >= m0) continue;
+      if (iz >= m2 || x0 + c >= K0) continue;
       const int fz = iz - h2;
-      const float4 G2 = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(fz, N)) * L + c]);
-      float4 Gm2 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (pair) Gm2 = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(-fz, N)) * L + T + c]);
-      const int kz = fz;
+      const int pf = dif_position<N>(wrap_freq(fz, N)), pm = dif_position<N>(wrap_freq(-fz, N));
+      const float4 P2 = *reinterpret_cast<const float4*>(&xs[pf * L + c]);
+      const float4 Pm2 = *reinterpret_cast<const float4*>(&xs[pm * L + c]);
+      float4 M2 = make_float4(0.f, 0.f, 0.f, 0.f), Mm2 = M2;
+      if (need_m) {
+        M2 = *reinterpret_cast<const float4*>(&xs[pf * L + T + c]);
+        Mm2 = *reinterpret_cast<const float4*>(&xs[pm * L + T + c]);
+      }
+      const float cz = c2[iz];
 #pragma unroll
       for (int hv = 0; hv < 2; ++hv) {
-        const int x = x0 + c + hv;
-        if (x >= m0) continue;
-        const float2 G = hv ? make_float2(G2.z, G2.w) : make_float2(G2.x, G2.y);
-        const float2 Gm = hv ? make_float2(Gm2.z, Gm2.w) : make_float2(Gm2.x, Gm2.y);
-        const float corr = c0[x] * cy * c2[iz];
-        const int kx = x - h0;
-        float s2 = 0.f;
-        if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
-          float qv[3];
-#pragma unroll
-          for (int b = 0; b < 3; ++b)
-            qv[b] = w.q0_f[b] + (float)kx * w.qs_f[0][b] + (float)ky * w.qs_f[1][b] + (float)kz * w.qs_f[2][b];
-          s2 = w.kappa_f * (qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2] + w.extra_f);
-        }
-        const int64_t q = ((int64_t)iz * m1 + iy) * m0 + x;
-        float ax, ay;
-        if (pair) {
-          const float ar = 0.5f * (G.x + Gm.x) * corr, ai = 0.5f * (G.y - Gm.y) * corr;
-          const float br = 0.5f * (G.y + Gm.y) * corr, bi = -0.5f * (G.x - Gm.x) * corr;
-          const float wa = species_weight<float>(w, sa, s2), wb = species_weight<float>(w, sb, s2);
-          ax = wa * ar + wb * br;
-          ay = wa * ai + wb * bi;
-          if (w.store_species) {
-            cs_species_frame[(int64_t)sa * nm + q] = make_float2(ar * w.wnorm_f, ai * w.wnorm_f);
-            cs_species_frame[(int64_t)sb * nm + q] = make_float2(br * w.wnorm_f, bi * w.wnorm_f);
-          }
-        } else {
-          const float wa = species_weight<float>(w, sa, s2);
-          ax = wa * G.x * corr;
-          ay = wa * G.y * corr;
-          if (w.store_species)
-            cs_species_frame[(int64_t)sa * nm + q] = make_float2(G.x * corr * w.wnorm_f, G.y * corr * w.wnorm_f);
-        }
+        const int x = x0 + c + hv;       // P column (beyond m0: only its mirror is a mode)
+        if (x >= K0) continue;
+        const float2 P = hv ? make_float2(P2.z, P2.w) : make_float2(P2.x, P2.y);
+        const float2 Pm = hv ? make_float2(Pm2.z, Pm2.w) : make_float2(Pm2.x, Pm2.y);
+        const float2 M = hv ? make_float2(M2.z, M2.w) : make_float2(M2.x, M2.y);
+        const float2 Mm = hv ? make_float2(Mm2.z, Mm2.w) : make_float2(Mm2.x, Mm2.y);
+        // P mode (iy, x, iz): G(k) on the P line, G(-k) on the M line at -fz
+        float2 a = make_float2(0.f, 0.f);
+        if (x < m0)
+          a = zpass_mode(P, Mm, pair, sa, sb, c0[x] * cy * cz, x - h0, ky, fz, w,
+                         ((int64_t)iz * m1 + iy) * m0 + x, nm, cs_species_frame);
+        // M mode (iym, 2h0 - x, iz): G(k) on the M line, G(-k) on the P line at -fz
+        float2 b = make_float2(0.f, 0.f);
+        const int xm = 2 * h0 - x;
+        if (mrow && xm < m0)
+          b = zpass_mode(M, Pm, pair, sa, sb, c0[xm] * cym * cz, xm - h0, kym, fz, w,
+                         ((int64_t)iz * m1 + iym) * m0 + xm, nm, cs_species_frame);
         if (hv) {
-          acc[p].z += ax;
-          acc[p].w += ay;
+          acc[p].z += a.x;
+          acc[p].w += a.y;
+          accm[p].z += b.x;
+          accm[p].w += b.y;
         } else {
-          acc[p].x += ax;
-          acc[p].y += ay;
+          acc[p].x += a.x;
+          acc[p].y += a.y;
+          accm[p].x += b.x;
+          accm[p].y += b.y;
         }
       }
     }
@@ -839,10 +867,16 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     const int e = tid + 256 * p;
     const int c = 2 * (e % TP), iz = e / TP;
     const int x = x0 + c;
-    if (iz >= m2 || x >= m0) continue;
+    if (iz >= m2 || x >= K0) continue;
     float2* q = cs_frame + ((int64_t)iz * m1 + iy) * m0 + x;
-    q[0] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
+    if (x < m0) q[0] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
     if (x + 1 < m0) q[1] = make_float2(acc[p].z * w.wnorm_f, acc[p].w * w.wnorm_f);
+    if (mrow) {
+      float2* qm = cs_frame + ((int64_t)iz * m1 + iym) * m0;
+      const int xm = 2 * h0 - x;   // in [0, 2 h0]; the column x + 1 mirrors to xm - 1
+      if (xm < m0) qm[xm] = make_float2(accm[p].x * w.wnorm_f, accm[p].y * w.wnorm_f);
+      if (x + 1 < K0 && xm - 1 < m0) qm[xm - 1] = make_float2(accm[p].z * w.wnorm_f, accm[p].w * w.wnorm_f);
+    }
   }
 }
 
@@ -889,7 +923,9 @@ static int launch_prune_z(const PruneLaunch& p, const WeightArgs& w, float2* csf
   constexpr int T = zpass_cols<N>();
   const size_t sm = pass_smem<N>(2 * T);
   cudaFuncSetAttribute(fftz_dif_deconv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  fftz_dif_deconv_kernel<N><<<dim3((unsigned)((p.m[0] + T - 1) / T), (unsigned)p.m[1]), 256, sm, p.s>>>(
+  const int rows = std::min(p.m[1], p.h[1] + 1);   // ky rows iy <= h1; each also forms 2 h1 - iy
+  // x tiles cover the K0 = 2 h0 + 1 kept columns: column 2 h0 is the mirror of mode column 0
+  fftz_dif_deconv_kernel<N><<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)rows), 256, sm, p.s>>>(
       p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.h[0], p.h[1], p.h[2], p.ngroups, p.tw[2],
       p.c[0], p.c[1], p.c[2], w, csf, css);
   MPSQ_LAUNCH_CHECK();
