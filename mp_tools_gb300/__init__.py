@@ -6,6 +6,7 @@ normalisations), the .dat/.par readers, synthetic workload generators and the jo
 """
 from . import _lib
 from ._lib import BULK, CELL, FP32, FP64, MpsqError, load
-from .sqom import QGrid, SqomJob, TimeAxis
+from .sqom import QGrid, SqomJob, TimeAxis, speckle_filter
 
-__all__ = ["load", "QGrid", "SqomJob", "TimeAxis", "MpsqError", "FP32", "FP64", "CELL", "BULK"]
+__all__ = ["load", "QGrid", "SqomJob", "TimeAxis", "speckle_filter", "MpsqError", "FP32", "FP64",
+           "CELL", "BULK"]
