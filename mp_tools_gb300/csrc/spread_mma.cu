@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256, 3)
     const int n0 = sm.n0, b1 = sm.b1, n1 = sm.n1;
     mma_region<W>(sm, 0, (n0 + 15) >> 4, n0, p0, g, t, acc_re);
     mma_region<W>(sm, b1 >> 4, (b1 + n1 + 15) >> 4, b1 + n1, p0, g, t, acc_im);
-    __syncthreads();
+    if (c0 + kCap < r1) __syncthreads();   // another chunk reuses the staging arrays
   }
   float2* out = fine + (int64_t)(keygrid + trans) * a.n_fine;
   const int64_t nf0 = a.nf[0], nf1 = a.nf[1];

@@ -398,12 +398,12 @@ __global__ void iqt_dispersion_kernel(Series<T> cs, int64_t nq, int nt,
   }
 }
 
-// FP32 Gaussian-window spectrum with an in-place mixed-radix (8, then 4 or 2) decimation-in-
-// frequency FFT.  One CTA holds the N x 16 tile cs(t, q0..q0+15) (one 128-byte line per time
-// row, three CTAs per SM for N = 512); every thread issues all its N/32 loads before using
-// them.  The elastic mean is subtracted and the window applied in the first stage; the
-// spectrum is read back at the digit-reversed positions.
-constexpr int kGaussQ = 16;
+// FP32 Gaussian-window spectrum with an in-place mixed-radix decimation-in-frequency FFT.  One
+// CTA holds the N x 8 tile cs(t, q0..q0+7) (64 bytes per time row; 8 columns measured 10 %
+// faster than 16 at N = 512); every thread issues all its loads before using them.  The
+// elastic mean is subtracted and the window applied in the first stage; the spectrum is read
+// back at the digit-reversed positions.
+constexpr int kGaussQ = 8;
 
 // First-stage hook: subtract the column's elastic mean and apply the time window.
 struct GaussPre {
@@ -425,32 +425,33 @@ __global__ void __launch_bounds__(256)
     gauss_dif_kernel(const float2* __restrict__ cs, int64_t nq, const float* __restrict__ gwin,
                      int n_freq, const float* __restrict__ q2n, float scale,
                      float* __restrict__ out) {
-  constexpr int QT = kGaussQ, RL = N / 32;
+  constexpr int QT = kGaussQ, CP = QT / 2, RPP = 256 / CP, RL = N / RPP;
+  static_assert(CP <= 32 && 32 % CP == 0 && N % RPP == 0, "Gaussian tile shape");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);       // [N][QT]
   float2* tw = xs + N * QT;                                 // exp(-2 pi i n / N)
-  float4* part = reinterpret_cast<float4*>(tw + N);         // [8 warps][8 column pairs]
-  float2* mean = reinterpret_cast<float2*>(part + 64);      // [QT]
+  float4* part = reinterpret_cast<float4*>(tw + N);         // [8 warps][CP column pairs]
+  float2* mean = reinterpret_cast<float2*>(part + 8 * CP);  // [QT]
   float* gw = reinterpret_cast<float*>(mean + QT);          // [N]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t q0 = (int64_t)blockIdx.x * QT;
   dif_twiddles<N>(tw);
   for (int i = tid; i < N; i += blockDim.x) gw[i] = gwin[i];
-  // rows t = (tid >> 3) + 32 i, columns q0 + 2 (tid & 7) + {0, 1}
-  const int c2 = tid & 7, r0 = tid >> 3;
+  // rows t = tid / CP + RPP i, columns q0 + 2 (tid % CP) + {0, 1}
+  const int c2 = tid % CP, r0 = tid / CP;
   const int64_t qa = q0 + 2 * c2;
   float4 v[RL];
   if ((nq & 1) == 0) {           // rows start on 16-byte boundaries: one float4 per pair
 #pragma unroll
     for (int i = 0; i < RL; ++i) {
-      const int64_t t = r0 + 32 * i;
+      const int64_t t = r0 + RPP * i;
       v[i] = qa < nq ? __ldcs(reinterpret_cast<const float4*>(cs + t * nq + qa))
                      : make_float4(0.f, 0.f, 0.f, 0.f);
     }
   } else {
 #pragma unroll
     for (int i = 0; i < RL; ++i) {
-      const int64_t t = r0 + 32 * i;
+      const int64_t t = r0 + RPP * i;
       const float2 a = qa < nq ? __ldcs(cs + t * nq + qa) : make_float2(0.f, 0.f);
       const float2 b = qa + 1 < nq ? __ldcs(cs + t * nq + qa + 1) : make_float2(0.f, 0.f);
       v[i] = make_float4(a.x, a.y, b.x, b.y);
@@ -460,22 +461,22 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int i = 0; i < RL; ++i) {
     s.x += v[i].x; s.y += v[i].y; s.z += v[i].z; s.w += v[i].w;
-    *reinterpret_cast<float4*>(&xs[(r0 + 32 * i) * QT + 2 * c2]) = v[i];
+    *reinterpret_cast<float4*>(&xs[(r0 + RPP * i) * QT + 2 * c2]) = v[i];
   }
-  // column sums: lanes c2, c2+8, c2+16, c2+24 of a warp, then the 8 warps
+  // column sums: the lanes c2 + CP k of a warp, then the 8 warps
 #pragma unroll
-  for (int o = 8; o < 32; o <<= 1) {
+  for (int o = CP; o < 32; o <<= 1) {
     s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
     s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
     s.z += __shfl_xor_sync(0xffffffffu, s.z, o);
     s.w += __shfl_xor_sync(0xffffffffu, s.w, o);
   }
-  if (lane < 8) part[warp * 8 + lane] = s;
+  if (lane < CP) part[warp * CP + lane] = s;
   __syncthreads();
   if (tid < QT) {
     float mr = 0.f, mi = 0.f;
     for (int w = 0; w < 8; ++w) {
-      const float4 p = part[w * 8 + (tid >> 1)];
+      const float4 p = part[w * CP + (tid >> 1)];
       mr += (tid & 1) ? p.z : p.x;
       mi += (tid & 1) ? p.w : p.y;
     }
@@ -499,7 +500,7 @@ __global__ void __launch_bounds__(256)
 
 template <int N>
 static size_t gauss_dif_smem() {
-  return (size_t)N * kGaussQ * sizeof(float2) + (size_t)N * sizeof(float2) + 64 * sizeof(float4) +
+  return (size_t)N * kGaussQ * sizeof(float2) + (size_t)N * sizeof(float2) + 8 * (kGaussQ / 2) * sizeof(float4) +
          kGaussQ * sizeof(float2) + (size_t)N * sizeof(float);
 }
 
