@@ -158,6 +158,11 @@ typedef struct mpsq_job_desc {
   int32_t no_pruned_fft;     /* 0: FP32 volumes use the pruned three-pass fine-grid
                                 transform fused with the deconvolution; 1: cuFFT + separate
                                 deconvolution                                             */
+  int32_t stream_ordered;    /* 1: the job's device memory is allocated and freed in the order
+                                of its stream (stream-ordered allocation from the device's
+                                memory pool), so creating and destroying a job never waits
+                                for the device (concurrent jobs of a request server); one
+                                frame lane.  0: plain allocation, destroy waits for the job */
 } mpsq_job_desc;
 
 typedef struct mpsq_job mpsq_job;

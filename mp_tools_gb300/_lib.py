@@ -71,6 +71,7 @@ class JobDesc(C.Structure):
         ("store_species", C.c_int32),
         ("no_pack", C.c_int32),
         ("no_pruned_fft", C.c_int32),
+        ("stream_ordered", C.c_int32),
     ]
 
 

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fft_smem.cuh"
@@ -157,6 +158,25 @@ struct mpsq_job {
   cufftHandle oneph_fft = 0;
   bool have_oneph_fft = false;
 };
+
+// Device memory of a job: stream-ordered (from the device's memory pool, on the job's stream)
+// when the job was created with stream_ordered = 1, plain otherwise.
+static cudaError_t job_alloc(mpsq_job* j, void** ptr, size_t bytes) {
+  bytes = std::max<size_t>(bytes, 16);
+  return j->d.stream_ordered ? cudaMallocAsync(ptr, bytes, j->s) : cudaMalloc(ptr, bytes);
+}
+static void job_release(mpsq_job* j, void* ptr) {
+  if (!ptr) return;
+  if (j->d.stream_ordered)
+    cudaFreeAsync(ptr, j->s);
+  else
+    cudaFree(ptr);
+}
+static cudaError_t job_upload(mpsq_job* j, void* dst, const void* src, size_t bytes) {
+  // pageable source: the copy is staged before the call returns
+  return j->d.stream_ordered ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, j->s)
+                             : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
 
 namespace mpsq {
 
@@ -1013,31 +1033,31 @@ static int job_layout(const mpsq_job_desc* d, EsKernel* es, GridGeom* g, int* ng
 static void job_free(mpsq_job* j) {
   if (!j) return;
   if (j->have_fft) cufftDestroy(j->fft);
-  cudaFree(j->traj);
-  cudaFree(j->at_ind);
-  cudaFree(j->fine);
-  cudaFree(j->counts);
-  cudaFree(j->starts);
-  cudaFree(j->perm);
-  cudaFree(j->perm_counts);
-  cudaFree(j->perm_starts);
-  cudaFree(j->recs);
-  cudaFree(j->str);
-  for (int a = 0; a < 3; ++a) cudaFree(j->corr[a]);
-  cudaFree(j->cs);
-  cudaFree(j->cs_species);
-  cudaFree(j->err);
-  cudaFree(j->b1);
-  for (auto& t : j->tw) cudaFree(t);
-  cudaFree(j->fine2);
-  cudaFree(j->counts2);
-  cudaFree(j->starts2);
-  cudaFree(j->recs2);
-  cudaFree(j->str2);
-  cudaFree(j->b1_2);
+  job_release(j, j->traj);
+  job_release(j, j->at_ind);
+  job_release(j, j->fine);
+  job_release(j, j->counts);
+  job_release(j, j->starts);
+  job_release(j, j->perm);
+  job_release(j, j->perm_counts);
+  job_release(j, j->perm_starts);
+  job_release(j, j->recs);
+  job_release(j, j->str);
+  for (int a = 0; a < 3; ++a) job_release(j, j->corr[a]);
+  job_release(j, j->cs);
+  job_release(j, j->cs_species);
+  job_release(j, j->err);
+  job_release(j, j->b1);
+  for (auto& t : j->tw) job_release(j, t);
+  job_release(j, j->fine2);
+  job_release(j, j->counts2);
+  job_release(j, j->starts2);
+  job_release(j, j->recs2);
+  job_release(j, j->str2);
+  job_release(j, j->b1_2);
   if (j->have_oneph_fft) cufftDestroy(j->oneph_fft);
-  cudaFree(j->oneph_u);
-  cudaFree(j->oneph_base);
+  job_release(j, j->oneph_u);
+  job_release(j, j->oneph_base);
   if (j->fork) cudaEventDestroy(j->fork);
   if (j->join) cudaEventDestroy(j->join);
   if (j->s2) cudaStreamDestroy(j->s2);
@@ -1084,6 +1104,19 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   auto* j = new mpsq_job();
   j->d = *d;
   j->s = (cudaStream_t)stream;
+  if (d->stream_ordered) {
+    // keep memory that jobs give back in the pool for the next job (process-local setting)
+    static std::once_flag once;
+    std::call_once(once, [] {
+      int dev = 0;
+      cudaMemPool_t pool;
+      if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+      cudaGetLastError();
+    });
+  }
   int gof[MPSQ_MAX_SPECIES], cof[MPSQ_MAX_SPECIES], pr[MPSQ_MAX_SPECIES] = {0},
       sa[MPSQ_MAX_SPECIES] = {0}, sb[MPSQ_MAX_SPECIES] = {0}, pack = 0;
   int rc = job_layout(d, &j->es, &j->g, &j->ngroups, gof, cof, pr, sa, sb, &pack);
@@ -1206,7 +1239,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   const int64_t nkeys = (int64_t)a.ngrid * j->g.n_tiles;
   cudaError_t e = cudaSuccess;
   auto A = [&](void** ptr, size_t bytes) {
-    if (e == cudaSuccess) e = cudaMalloc(ptr, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess) e = job_alloc(j, ptr, bytes);
   };
   A((void**)&j->traj, (size_t)d->n_frames * d->n_atoms_frame * sizeof(float4));
   A(&j->fine, (size_t)a.ngrid * j->g.n_fine * cs);
@@ -1226,13 +1259,14 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
     A(&j->corr[k], c.size() * (prec == MPSQ_FP64 ? 8 : 4));
     if (e != cudaSuccess) break;
     if (prec == MPSQ_FP64) {
-      e = cudaMemcpy(j->corr[k], c.data(), c.size() * 8, cudaMemcpyHostToDevice);
+      e = job_upload(j, j->corr[k], c.data(), c.size() * 8);
     } else {
       std::vector<float> cf(c.begin(), c.end());
-      e = cudaMemcpy(j->corr[k], cf.data(), c.size() * 4, cudaMemcpyHostToDevice);
+      e = job_upload(j, j->corr[k], cf.data(), c.size() * 4);
     }
   }
-  if (e == cudaSuccess) e = cudaMemset(j->err, 0, sizeof(int));
+  if (e == cudaSuccess)
+    e = j->d.stream_ordered ? cudaMemsetAsync(j->err, 0, sizeof(int), j->s) : cudaMemset(j->err, 0, sizeof(int));
   if (e != cudaSuccess) {
     job_free(j);
     return fail(e == cudaErrorMemoryAllocation ? MPSQ_ERR_ALLOC : MPSQ_ERR_CUDA, "job_create: %s",
@@ -1247,16 +1281,15 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
       j->K[k] = 2 * j->h[k] + 1;
     }
     const int64_t n1 = j->g.nf[1], n2 = j->g.nf[2];
-    e = cudaMalloc(&j->b1, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
+    e = job_alloc(j, (void**)&j->b1, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       std::vector<float2> t(j->g.nf[k]);
       for (int64_t i = 0; i < j->g.nf[k]; ++i) {
         const double ang = -2.0 * M_PI * (double)i / (double)j->g.nf[k];
         t[i] = make_float2((float)std::cos(ang), (float)std::sin(ang));
       }
-      e = cudaMalloc(&j->tw[k], sizeof(float2) * t.size());
-      if (e == cudaSuccess)
-        e = cudaMemcpy(j->tw[k], t.data(), sizeof(float2) * t.size(), cudaMemcpyHostToDevice);
+      e = job_alloc(j, (void**)&j->tw[k], sizeof(float2) * t.size());
+      if (e == cudaSuccess) e = job_upload(j, j->tw[k], t.data(), sizeof(float2) * t.size());
     }
     if (e != cudaSuccess) {
       job_free(j);
@@ -1270,8 +1303,8 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
                          (size_t)j->cap * (rsize(prec) + cs) +
                          sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0];
     size_t free_b = 0, total_b = 0;
-    if (!(lanes && strcmp(lanes, "1") == 0) && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
-        extra * 4 < free_b) {
+    if (!d->stream_ordered && !(lanes && strcmp(lanes, "1") == 0) &&
+        cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && extra * 4 < free_b) {
       cudaError_t e2 = cudaStreamCreateWithFlags(&j->s2, cudaStreamNonBlocking);
       if (e2 == cudaSuccess) e2 = cudaEventCreateWithFlags(&j->fork, cudaEventDisableTiming);
       if (e2 == cudaSuccess) e2 = cudaEventCreateWithFlags(&j->join, cudaEventDisableTiming);
@@ -1312,9 +1345,11 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
 }
 
 extern "C" int mpsq_job_destroy(mpsq_job* j) {
-  if (j && j->s2) cudaStreamSynchronize(j->s2);
-  if (j && j->s) cudaStreamSynchronize(j->s);
-  job_free(j);
+  if (j && !j->d.stream_ordered) {
+    if (j->s2) cudaStreamSynchronize(j->s2);
+    if (j->s) cudaStreamSynchronize(j->s);
+  }
+  job_free(j);   // stream-ordered: the frees follow the job's queued work on its stream
   return MPSQ_OK;
 }
 
@@ -1339,7 +1374,7 @@ extern "C" int mpsq_job_set_frames(mpsq_job* j, const float* pos, int32_t first,
 
 extern "C" int mpsq_job_set_cell_index(mpsq_job* j, const int32_t* at_ind, int host) {
   if (!j || !at_ind) return fail(MPSQ_ERR_ARG, "set_cell_index: null pointer");
-  if (!j->at_ind) MPSQ_CUDA_TRY(cudaMalloc(&j->at_ind, (size_t)j->d.n_atoms_frame * sizeof(int4)));
+  if (!j->at_ind) MPSQ_CUDA_TRY(job_alloc(j, (void**)&j->at_ind, (size_t)j->d.n_atoms_frame * sizeof(int4)));
   MPSQ_CUDA_TRY(cudaMemcpyAsync(j->at_ind, at_ind, (size_t)j->d.n_atoms_frame * sizeof(int4),
                                 host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, j->s));
   return MPSQ_OK;
@@ -1487,7 +1522,7 @@ static int job_onephonon_t(mpsq_job* j, int32_t first, int32_t count, int32_t pl
   const int m0 = (int)j->d.n_modes[0], m1 = (int)j->d.n_modes[1];
   const int ns = j->d.n_species;
   const size_t usz = (size_t)ns * 2 * n1 * n2 * sizeof(C);
-  if (!j->oneph_u) MPSQ_CUDA_TRY(cudaMalloc(&j->oneph_u, usz));
+  if (!j->oneph_u) MPSQ_CUDA_TRY(job_alloc(j, &j->oneph_u, usz));
   if (!j->have_oneph_fft) {
     int n[2] = {n2, n1};
     MPSQ_CUFFT_TRY(cufftPlanMany(&j->oneph_fft, 2, n, nullptr, 1, n1 * n2, nullptr, 1, n1 * n2,
@@ -1543,7 +1578,7 @@ extern "C" int mpsq_job_transform_onephonon(mpsq_job* j, int32_t first, int32_t 
     return fail(MPSQ_ERR_ARG, "transform_onephonon: %d zones of %d cells exceed the %lld x %lld plane",
                 n_bz, nr[0], (long long)j->d.n_modes[0], (long long)j->d.n_modes[1]);
   if (!j->at_ind) return fail(MPSQ_ERR_STATE, "transform_onephonon: set the cell indices first");
-  if (!j->oneph_base) MPSQ_CUDA_TRY(cudaMalloc(&j->oneph_base, sizeof(float) * 3 * MPSQ_MAX_SPECIES));
+  if (!j->oneph_base) MPSQ_CUDA_TRY(job_alloc(j, (void**)&j->oneph_base, sizeof(float) * 3 * MPSQ_MAX_SPECIES));
   MPSQ_CUDA_TRY(cudaMemcpyAsync(j->oneph_base, at_base, sizeof(float) * 3 * j->d.n_species,
                                 cudaMemcpyHostToDevice, j->s));
   // (a host-to-device copy from pageable memory has left the caller's buffer on return)

@@ -1,0 +1,236 @@
+"""Request server for S(Q,omega) jobs on one GPU: continuous batching with admission by device
+memory.
+
+Requests arrive over time, each an MD trajectory (host memory) with its Q grid and weights.  A
+request is admitted as soon as an execution slot is free and its device footprint
+(``mpsq_job_estimate_bytes``: trajectory, fine grids, records, amplitude store) fits in what
+the admitted jobs leave of the budget; requests that could never fit are rejected, the others
+wait in arrival order.  Every admitted job runs on its own CUDA stream with stream-ordered
+device memory, so creating and closing a job never waits for the device, and the kernels of
+jobs that are in flight together overlap on the GPU (a job that arrives while others run starts
+at once instead of after them).  The host loop only launches work, polls completion events and
+admits the next requests.
+
+Per job: upload of the trajectory, the NUFFT of every frame and species with the species
+weights, total S(Q) and, for runs of at least 4 frames, E=const maps of the first frequency bins
+(mp_sqom's sliding-window form), all copied back to pinned host memory; the job's latency is the
+time from its arrival to the moment its results are on the host.  ``Server.run`` returns the
+results and the stream's statistics: p50/p99 latency, throughput in nonuniform points per
+second, completed / rejected counts and the longest queue.
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .sqom import QGrid, SqomJob, TimeAxis
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float                 # seconds after the start of the stream
+    frames: object                 # (F, N, 4) float32 host array / tensor (pinned: overlapped copy)
+    counts: list                   # atoms per species (species-major order of the frames)
+    grid: QGrid
+    job_kwargs: dict = field(default_factory=dict)   # SqomJob arguments (precision, eps, weights)
+    t_step: float = 0.01           # ps between frames (E=const maps)
+    n_econst: int = 4              # E=const bins returned when the run has >= 4 frames
+
+    @property
+    def n_frames(self) -> int:
+        return int(self.frames.shape[0])
+
+    @property
+    def nu_points(self) -> int:
+        return int(sum(self.counts)) * self.n_frames
+
+
+@dataclass
+class Result:
+    rid: int
+    sq: np.ndarray
+    sqw: np.ndarray | None        # (n_bins, n_Q) E=const maps, or None
+    arrival: float
+    admitted: float
+    done: float
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+class GpuExecutor:
+    """Runs a request as a stream-ordered SqomJob on its own stream."""
+
+    def estimate(self, req: Request) -> int:
+        d = SqomJob.describe(req.grid, species_counts=req.counts, n_frames=req.n_frames,
+                             n_atoms_frame=int(req.frames.shape[1]), stream_ordered=True,
+                             **req.job_kwargs)
+        out = (req.grid.n_modes * (1 + req.n_econst)) * 4
+        return SqomJob.estimate_bytes(d) + out
+
+    def start(self, req: Request):
+        import torch
+        stream = torch.cuda.Stream()
+        job = SqomJob(req.grid, species_counts=req.counts, n_frames=req.n_frames,
+                      n_atoms_frame=int(req.frames.shape[1]), stream=stream.cuda_stream,
+                      stream_ordered=True, **req.job_kwargs)
+        nq = req.grid.n_modes
+        F = req.n_frames
+        n_bins = 0
+        if F >= 4:
+            ta = TimeAxis(nfile=F, t_step=req.t_step)
+            n_bins = min(req.n_econst, ta.n_freq_max)
+        with torch.cuda.stream(stream):
+            dev_sq = torch.empty(nq, dtype=torch.float32, device="cuda")
+            dev_sqw = torch.empty((n_bins, nq), dtype=torch.float32, device="cuda") if n_bins else None
+        host_sq = torch.empty(nq, dtype=torch.float32, pin_memory=True)
+        host_sqw = torch.empty((n_bins, nq), dtype=torch.float32, pin_memory=True) if n_bins else None
+        job.set_frames(req.frames)                 # pinned host -> device on the job's stream
+        job.transform()
+        job.sq_total(out=dev_sq)
+        for b in range(n_bins):
+            job.sqw_econst(ta, b + 1, out=dev_sqw[b])
+        with torch.cuda.stream(stream):
+            host_sq.copy_(dev_sq, non_blocking=True)
+            if n_bins:
+                host_sqw.copy_(dev_sqw, non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(stream)
+        return {"job": job, "stream": stream, "done": done, "sq": host_sq, "sqw": host_sqw,
+                "dev": (dev_sq, dev_sqw), "frames": req.frames}
+
+    def done(self, h) -> bool:
+        return h["done"].query()
+
+    def finish(self, h):
+        job = h["job"]
+        job.sync()                                 # completed already: checks the error flag
+        job.close()                                # stream-ordered frees, no device wait
+        sq = h["sq"].numpy().copy()
+        sqw = h["sqw"].numpy().copy() if h["sqw"] is not None else None
+        return sq, sqw
+
+
+class Server:
+    """Admission by memory and execution slots, first come first served; see the module
+    docstring.  `executor` provides estimate(req) -> bytes, start(req) -> handle,
+    done(handle) -> bool and finish(handle) -> (sq, sqw)."""
+
+    def __init__(self, executor=None, budget_bytes: int | None = None, max_active: int = 8,
+                 poll_s: float = 2e-4, clock=time.perf_counter, sleep=time.sleep):
+        self.ex = executor if executor is not None else GpuExecutor()
+        if budget_bytes is None:
+            import torch
+            free, total = torch.cuda.mem_get_info()
+            budget_bytes = int(0.8 * free)
+        self.budget = int(budget_bytes)
+        self.max_active = int(max_active)
+        self.poll_s = poll_s
+        self.clock = clock
+        self.sleep = sleep
+
+    def run(self, requests):
+        pending = deque(sorted(requests, key=lambda r: (r.arrival, r.rid)))
+        queue: deque = deque()
+        active = []                # (req, handle, bytes, admitted)
+        results: dict[int, Result] = {}
+        rejected, waited = [], set()
+        used = peak = 0
+        max_queue = 0
+        t0 = self.clock()
+        first = pending[0].arrival if pending else 0.0
+        while pending or queue or active:
+            now = self.clock() - t0
+            while pending and pending[0].arrival <= now:
+                r = pending.popleft()
+                b = self.ex.estimate(r)
+                if b > self.budget:
+                    rejected.append(r.rid)
+                else:
+                    queue.append((r, b))
+            # completions first: they free memory and slots
+            still = []
+            for r, h, b, adm in active:
+                if self.ex.done(h):
+                    sq, sqw = self.ex.finish(h)
+                    t = self.clock() - t0
+                    results[r.rid] = Result(r.rid, sq, sqw, r.arrival, adm, t)
+                    used -= b
+                else:
+                    still.append((r, h, b, adm))
+            active = still
+            # admissions in arrival order (the head of the queue blocks the rest)
+            while queue and len(active) < self.max_active and used + queue[0][1] <= self.budget:
+                r, b = queue.popleft()
+                adm = self.clock() - t0
+                used += b
+                peak = max(peak, used)
+                active.append((r, self.ex.start(r), b, adm))
+            for r, _ in queue:            # could not start on arrival: waited for memory/slot
+                waited.add(r.rid)
+            max_queue = max(max_queue, len(queue))
+            if not queue and not active and pending:
+                self.sleep(max(0.0, min(pending[0].arrival - (self.clock() - t0), 0.05)))
+            elif active or queue:
+                self.sleep(self.poll_s)
+        wall = (self.clock() - t0) - first
+        lat = np.array([results[k].latency for k in sorted(results)])
+        pts = sum(r.nu_points for r in requests if r.rid in results)
+        stats = {
+            "completed": len(results), "rejected": len(rejected), "rejected_ids": rejected,
+            "queued": len(waited), "max_queue": max_queue, "budget_bytes": self.budget,
+            "peak_admitted_bytes": peak, "max_active": self.max_active,
+            "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "mean_s": float(lat.mean()) if len(lat) else None,
+            "wall_s": wall, "nu_pts_per_s": pts / wall if wall > 0 else None,
+        }
+        return results, stats
+
+
+# ------------------------------------------------------------------ synthetic request stream
+ABO3_B = [0.507, 0.716, 0.5803, 0.5803, 0.5803]   # neutron b_coh (10^-12 cm): A, B, O, O, O
+
+
+def abo3_request(rid, arrival, edge, n_frames, zones, rng, precision=_lib.FP32, eps=1e-5,
+                 a=4.19, sigma=(0.05, 0.08), pinned=True):
+    """One ABO3 supercell job: edge^3 cells (5 edge^3 atoms), n_frames frames of independent
+    Gaussian displacements (sigma A/B and O in Angstrom) around the ideal sites, a Q volume of
+    `zones` Brillouin zones per axis, neutron weights."""
+    from . import synth
+    cells, _ = synth.abo3_cells(edge)
+    nc = len(cells)
+    base = np.concatenate([cells + synth.ABO3_BASIS[s] for s in range(5)]).astype(np.float32)
+    sig = np.repeat(np.array([sigma[0], sigma[0], sigma[1], sigma[1], sigma[1]]) / a, nc)
+    fr = np.zeros((n_frames, 5 * nc, 4), np.float32)
+    fr[:, :, :3] = base[None] + (rng.standard_normal((n_frames, 5 * nc, 3)) * sig[None, :, None])
+    if pinned:
+        import torch
+        t = torch.from_numpy(fr).pin_memory()
+    else:
+        t = fr
+    grid = QGrid(_lib.CELL, (edge,) * 3, n_bz=zones, a_par=(a,) * 3, ndim=3)
+    kw = dict(precision=precision, eps=eps, weight_mode=_lib.WEIGHT_NEUTRON, b_coh=ABO3_B)
+    return Request(rid, float(arrival), t, [nc] * 5, grid, kw)
+
+
+def poisson_stream(n_jobs, rate_hz, seed, edge=(16, 100), frames=(1, 256), zones=(4, 8),
+                   precision=_lib.FP32, eps=1e-5, pinned=True):
+    """The serving stream: n_jobs ABO3 requests with Poisson arrivals at rate_hz, edge, frame
+    count and zones uniform in the given inclusive ranges (seeded)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n_jobs):
+        t += rng.exponential(1.0 / rate_hz)
+        e = int(rng.integers(edge[0], edge[1] + 1))
+        f = int(rng.integers(frames[0], frames[1] + 1))
+        z = int(rng.integers(zones[0], zones[1] + 1))
+        out.append(abo3_request(i, t, e, f, z, rng, precision=precision, eps=eps, pinned=pinned))
+    return out

@@ -190,17 +190,17 @@ class TimeAxis:
 class SqomJob:
     """One S(Q,omega) job on the GPU (device-resident trajectory, amplitudes and grids)."""
 
-    def __init__(self, grid: QGrid, *, species_counts, n_frames: int, precision: int = _lib.FP32,
+    @staticmethod
+    def describe(grid: QGrid, *, species_counts, n_frames: int, precision: int = _lib.FP32,
                  eps: float = 1e-6, weight_mode: int = _lib.WEIGHT_UNIT, b_coh=None, xff=None,
                  ff_convention: int = _lib.FF_MP_SQOM, mask=None, window: bool = False,
                  phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
-                 no_pruned_fft: bool = False,
-                 n_atoms_frame: int | None = None, use_range: bool = False, eps_x: float = 0.1,
-                 stream: int | None = None):
-        L = _lib.load()
-        self.grid = grid
-        self.species_counts = [int(n) for n in species_counts]
-        S = len(self.species_counts)
+                 no_pruned_fft: bool = False, n_atoms_frame: int | None = None,
+                 use_range: bool = False, eps_x: float = 0.1, stream_ordered: bool = False):
+        """The job descriptor (mpsq_job_desc) of these arguments, without creating the job
+        (for estimate_bytes and admission control)."""
+        counts = [int(n) for n in species_counts]
+        S = len(counts)
         if S < 1 or S > _lib.MAX_SPECIES:
             raise ValueError("1..16 species supported")
         d = _lib.JobDesc()
@@ -224,7 +224,7 @@ class SqomJob:
         d.bulk_nsuper1 = int(grid.nsuper == 1)
         d.spatial_window = int(window)
         d.n_species = S
-        off = np.concatenate([[0], np.cumsum(self.species_counts)])
+        off = np.concatenate([[0], np.cumsum(counts)])
         for s in range(S + 1):
             d.species_offset[s] = int(off[s])
         mask = [1] * S if mask is None else list(mask)
@@ -250,6 +250,28 @@ class SqomJob:
         d.store_species = int(store_species)
         d.no_pack = int(no_pack)
         d.no_pruned_fft = int(no_pruned_fft)
+        # device memory from the stream-ordered pool: creating and closing the job never wait
+        # for the device (many concurrent jobs, as in the request server)
+        d.stream_ordered = int(stream_ordered)
+        return d
+
+    def __init__(self, grid: QGrid, *, species_counts, n_frames: int, precision: int = _lib.FP32,
+                 eps: float = 1e-6, weight_mode: int = _lib.WEIGHT_UNIT, b_coh=None, xff=None,
+                 ff_convention: int = _lib.FF_MP_SQOM, mask=None, window: bool = False,
+                 phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
+                 no_pruned_fft: bool = False,
+                 n_atoms_frame: int | None = None, use_range: bool = False, eps_x: float = 0.1,
+                 stream: int | None = None, stream_ordered: bool = False):
+        L = _lib.load()
+        self.grid = grid
+        self.species_counts = [int(n) for n in species_counts]
+        d = SqomJob.describe(grid, species_counts=species_counts, n_frames=n_frames,
+                             precision=precision, eps=eps, weight_mode=weight_mode, b_coh=b_coh,
+                             xff=xff, ff_convention=ff_convention, mask=mask, window=window,
+                             phase_rounding=phase_rounding, store_species=store_species,
+                             no_pack=no_pack, no_pruned_fft=no_pruned_fft,
+                             n_atoms_frame=n_atoms_frame, use_range=use_range, eps_x=eps_x,
+                             stream_ordered=stream_ordered)
         self.desc = d
         self.n_frames = int(n_frames)
         self.n_atoms_frame = d.n_atoms_frame
@@ -491,15 +513,17 @@ class SqomJob:
         n_slow, n_fast = res.shape if dispersion else self._plane_shape("speckle filter")
         check(_lib.load().mpsq_speckle_filter(C.c_void_p(ptr(res)), int(n_fast), int(n_slow),
                                               float(s_trig), int(not dispersion), float(post_scale),
-                                              int(host), None), "speckle_filter")
+                                              int(host), C.c_void_p(self._stream or None)),
+              "speckle_filter")
         return res
 
     def sqw_econst(self, taxis: TimeAxis, j_freq: int, q2_norm=None, normalize=True,
-                   t_wind=None, atom_pair=None, s_trig: float = 0.0) -> np.ndarray:
+                   t_wind=None, atom_pair=None, s_trig: float = 0.0, out=None) -> np.ndarray:
         """E=const map for 1-based bin j_freq (:1437-1478), normalised as :1527, :1575-1576.
         atom_pair=(a, b): the map of the raw amplitudes of species a + b (0-based; :1460-1464;
         needs store_species), where q2_norm does not apply.  s_trig > 0: speckle filter
-        (:1531-1570) between the two normalisations, as the reference applies it."""
+        (:1531-1570) between the two normalisations, as the reference applies it.  out: a
+        device tensor, or a host tensor filled asynchronously (see sq_total)."""
         w = np.ascontiguousarray(taxis.window() if t_wind is None else t_wind, f32)
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
         scale = 1.0 / (0.5 * taxis.n_frame * taxis.n_int)
@@ -508,17 +532,24 @@ class SqomJob:
             self._plane_shape("speckle filter")
         else:
             scale *= post
-        res = np.empty(self.grid.n_modes, f32)
+        res, host, copy_to = self._target(out, "econst", (self.grid.n_modes,))
+        if res is None:
+            res = np.empty(self.grid.n_modes, f32)
         L = _lib.load()
         if atom_pair is None:
             check(L.mpsq_job_sqw_econst(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
-                                        C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), 1),
+                                        C.c_void_p(ptr(q2)), scale, C.c_void_p(ptr(res)), host),
                   "sqw_econst")
         else:
             check(L.mpsq_job_sqw_econst_pair(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
                                              int(atom_pair[0]), int(atom_pair[1]), scale,
-                                             C.c_void_p(ptr(res)), 1), "sqw_econst_pair")
-        return self._speckle(res, s_trig, False, post) if s_trig > 0 else res
+                                             C.c_void_p(ptr(res)), host), "sqw_econst_pair")
+        if s_trig > 0:
+            res = self._speckle(res, s_trig, False, post, bool(host))
+        if copy_to is not None:
+            self._copy_out(res, copy_to)
+            return copy_to
+        return res
 
     def sqw_dispersion(self, taxis: TimeAxis, q_index, n_freq=None, q2_norm=None,
                        normalize=True, t_wind=None, atom_pair=None, s_trig: float = 0.0) -> np.ndarray:

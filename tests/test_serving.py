@@ -1,0 +1,129 @@
+"""Request server (continuous batching, admission by device memory).
+
+CPU: the scheduler against a simulated executor and clock: arrival order, the memory budget
+and the slot count are never exceeded, requests too large for the budget are rejected, jobs
+that arrive while others run start as soon as memory frees, latency percentiles.
+GPU: a mixed stream of ABO3 jobs of different sizes and frame counts, admitted under a budget
+that forces queueing, gives every job the same S(Q) and E=const maps as the job run alone
+(relative l2 1e-5: FP32, record order within a tile follows the binning atomics)."""
+import numpy as np
+import pytest
+
+from mp_tools_gb300 import serve
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def clock(self):
+        return self.t
+
+    def sleep(self, dt):
+        self.t += max(dt, 1e-4)
+
+
+class FakeExecutor:
+    """Each request carries .mem (bytes) and .dur (seconds on the device)."""
+
+    def __init__(self, clk):
+        self.clk = clk
+        self.running = {}
+        self.max_used = 0
+        self.used = 0
+        self.max_concurrent = 0
+
+    def estimate(self, req):
+        return req.mem
+
+    def start(self, req):
+        self.used += req.mem
+        self.max_used = max(self.max_used, self.used)
+        self.running[req.rid] = self.clk.t + req.dur
+        self.max_concurrent = max(self.max_concurrent, len(self.running))
+        return req
+
+    def done(self, h):
+        return self.clk.t >= self.running[h.rid]
+
+    def finish(self, h):
+        del self.running[h.rid]
+        self.used -= h.mem
+        return np.full(3, float(h.rid)), None
+
+
+def _req(rid, arrival, mem, dur):
+    r = serve.Request(rid, arrival, np.zeros((1, 10, 4), np.float32), [10], grid=None)
+    r.mem, r.dur = mem, dur
+    return r
+
+
+def test_scheduler_budget_slots_and_rejection():
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    reqs = [_req(0, 0.00, 40, 1.0), _req(1, 0.01, 40, 1.0), _req(2, 0.02, 40, 0.5),
+            _req(3, 0.03, 500, 0.1), _req(4, 0.04, 10, 0.2), _req(5, 3.0, 30, 0.1)]
+    srv = serve.Server(ex, budget_bytes=100, max_active=3, clock=clk.clock, sleep=clk.sleep)
+    res, st = srv.run(reqs)
+    assert st["rejected_ids"] == [3]                       # larger than the whole budget
+    assert sorted(res) == [0, 1, 2, 4, 5]
+    assert ex.max_used <= 100 and st["peak_admitted_bytes"] <= 100
+    assert ex.max_concurrent <= 3
+    # 2 needs 40 more than 0 and 1 leave: it waits until one of them ends; 4 waits behind it
+    assert res[2].admitted >= 1.0 - 1e-9 and res[4].admitted >= res[2].admitted
+    assert st["queued"] >= 2 and st["max_queue"] >= 2
+    assert res[5].admitted == pytest.approx(3.0, abs=1e-3)  # an idle server starts at once
+    for r in res.values():
+        assert np.all(r.sq == r.rid)
+    lat = np.array([res[k].latency for k in sorted(res)])
+    assert st["p50_s"] == pytest.approx(np.percentile(lat, 50))
+    assert st["p99_s"] == pytest.approx(np.percentile(lat, 99))
+
+
+def test_scheduler_overlaps_jobs_that_fit():
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    reqs = [_req(i, 0.001 * i, 10, 1.0) for i in range(4)]
+    res, st = serve.Server(ex, budget_bytes=100, max_active=8, clock=clk.clock,
+                           sleep=clk.sleep).run(reqs)
+    assert ex.max_concurrent == 4 and st["queued"] == 0
+    assert max(r.done for r in res.values()) < 1.1      # all four ran together
+
+
+@pytest.mark.gpu
+def test_gpu_results_same_alone_and_in_the_mix(cuda):
+    from mp_tools_gb300 import _lib
+    rng = np.random.default_rng(7)
+    specs = [(0.000, 4, 8, 2), (0.002, 6, 1, 2), (0.004, 5, 16, 2), (0.006, 8, 4, 2),
+             (0.008, 4, 6, 3), (0.010, 6, 12, 2)]
+    reqs = [serve.abo3_request(i, t, e, f, z, rng) for i, (t, e, f, z) in enumerate(specs)]
+    ex = serve.GpuExecutor()
+    est = [ex.estimate(r) for r in reqs]
+    budget = int(2.2 * max(est))                          # forces some queueing
+    mixed, st = serve.Server(ex, budget_bytes=budget, max_active=4).run(reqs)
+    assert st["completed"] == len(reqs) and st["rejected"] == 0
+    assert st["peak_admitted_bytes"] <= budget
+    alone = {}
+    for r in reqs:                                         # one job at a time
+        a, _ = serve.Server(ex, budget_bytes=budget, max_active=1).run(
+            [serve.Request(r.rid, 0.0, r.frames, r.counts, r.grid, r.job_kwargs)])
+        alone[r.rid] = a[r.rid]
+    for k in alone:
+        m, a = mixed[k], alone[k]
+        assert np.linalg.norm(m.sq - a.sq) <= 1e-5 * np.linalg.norm(a.sq), k
+        if a.sqw is None:
+            assert m.sqw is None
+        else:
+            assert np.linalg.norm(m.sqw - a.sqw) <= 1e-5 * np.linalg.norm(a.sqw), k
+    # and against the plain (job-at-a-time) API
+    from mp_tools_gb300.sqom import SqomJob
+    r = reqs[2]
+    job = SqomJob(r.grid, species_counts=r.counts, n_frames=r.n_frames, **r.job_kwargs)
+    try:
+        job.set_frames(r.frames)
+        job.transform()
+        sq = job.sq_total()
+    finally:
+        job.close()
+    assert np.linalg.norm(mixed[2].sq - sq) <= 1e-5 * np.linalg.norm(sq)
+    assert _lib.load().mpsq_launch_count() > 0
