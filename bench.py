@@ -464,6 +464,63 @@ def run_profile_case(args):
     job.close()
 
 
+def run_serving(args):
+    """Serving stream (C3 shape, scaled so that it finishes in about a minute): ABO3 jobs with
+    Poisson arrivals, edge / frames / zones uniform in the given ranges, FP32 at eps 1e-5,
+    through the request server (continuous batching, admission by device memory), then the
+    same jobs one at a time in FP64 on a bounded subset.  One JSON line with p50/p99 latency,
+    throughput and the completed / rejected / queued counts."""
+    import torch
+    from mp_tools_gb300 import _lib, serve
+    import dataclasses
+    edge = tuple(int(x) for x in args.serving_edge.split(","))
+    frames = tuple(int(x) for x in args.serving_frames.split(","))
+    zones = tuple(int(x) for x in args.serving_zones.split(","))
+    reqs = serve.poisson_stream(args.serving_jobs, 1.0, SEED + 3, edge=edge, frames=frames,
+                                zones=zones)
+    warm = serve.poisson_stream(2, 100.0, SEED + 4, edge=(edge[0], edge[0]), frames=(4, 4),
+                                zones=(zones[0], zones[0]))
+    serve.Server(max_active=args.serving_slots).run(warm)          # builds, pools, streams
+    torch.cuda.synchronize()
+    # capacity: the whole stream at once; then Poisson arrivals at load x capacity
+    _, cap = serve.Server(max_active=args.serving_slots).run(
+        [dataclasses.replace(r, arrival=0.0) for r in reqs])
+    capacity = cap["nu_pts_per_s"]
+    rate = args.serving_load * capacity / float(np.mean([r.nu_points for r in reqs]))
+    if args.serving_rate > 0:
+        rate = args.serving_rate
+    rng = np.random.default_rng(SEED + 5)
+    t = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    reqs = [dataclasses.replace(r, arrival=float(a)) for r, a in zip(reqs, t)]
+    srv = serve.Server(max_active=args.serving_slots)
+    res, st = srv.run(reqs)
+    # the baseline of the config: one job at a time in FP64 (a bounded subset)
+    sub = reqs[: args.serving_fp64_jobs]
+    plain = [serve.Request(r.rid, 0.0, r.frames, r.counts, r.grid,
+                           dict(r.job_kwargs, precision=_lib.FP64)) for r in sub]
+    t0 = time.perf_counter()
+    serve.Server(max_active=1).run(plain)
+    t_fp64 = time.perf_counter() - t0
+    pts_sub = sum(r.nu_points for r in sub)
+    out = {"metric": "job latency p50/p99 (s), serving stream", "impl": "mpsq",
+           "unit": "s", "data": "synthetic (seeded ABO3 supercells, Gaussian displacements)",
+           "config": {"workload": f"{len(reqs)} ABO3 jobs, Poisson arrivals at {rate:.1f} /s "
+                                  f"(offered load {args.serving_load:g} x the measured capacity "
+                                  f"{capacity:.3g} NU pts/s), edge {edge}, frames {frames}, "
+                                  f"zones {zones}, FP32 eps 1e-5, neutron weights, S(Q) + "
+                                  f"up to 4 E=const maps per job",
+                      "slots": args.serving_slots, "budget_bytes": st["budget_bytes"]},
+           "capacity_nu_pts_s": capacity, "capacity_p50_s": cap["p50_s"],
+           "capacity_p99_s": cap["p99_s"],
+           "p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"],
+           "throughput_nu_pts_s": st["nu_pts_per_s"], "wall_s": st["wall_s"],
+           "completed": st["completed"], "rejected": st["rejected"], "queued": st["queued"],
+           "max_queue": st["max_queue"], "peak_admitted_bytes": st["peak_admitted_bytes"],
+           "fp64_one_at_a_time": {"jobs": len(sub), "nu_pts_s": pts_sub / t_fp64,
+                                  "wall_s": t_fp64}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-case", action="store_true",
@@ -477,8 +534,21 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--serving", action="store_true",
+                    help="run the serving stream (request server) instead of the batched job")
+    ap.add_argument("--serving-jobs", type=int, default=40)
+    ap.add_argument("--serving-rate", type=float, default=0.0,
+                    help="arrivals per second (0: serving-load x the measured capacity)")
+    ap.add_argument("--serving-load", type=float, default=1.0)
+    ap.add_argument("--serving-edge", default="8,32")
+    ap.add_argument("--serving-frames", default="1,64")
+    ap.add_argument("--serving-zones", default="2,4")
+    ap.add_argument("--serving-slots", type=int, default=8)
+    ap.add_argument("--serving-fp64-jobs", type=int, default=6)
     args = ap.parse_args()
-    if args.profile_case:
+    if args.serving:
+        run_serving(args)
+    elif args.profile_case:
         run_profile_case(args)
     elif args.impl == "reference":
         run_reference(args)
