@@ -612,10 +612,10 @@ __global__ void oneph_expand_kernel(const typename Cplx<T>::type* __restrict__ u
 //      weights, cs(t, Q)
 // K = 2h+1; frequency f is stored at index f + h.
 
-// All three passes keep a tile of 16 (X, Y) or 2 x 16 (Z) lines of length N in shared memory
-// as [position][line] (lines fastest, so every warp access covers whole 128-byte rows), issue
-// all of a thread's global loads before storing any, transform in place (dif_lines) and read
-// the kept frequencies at their digit-reversed positions.
+// All three passes keep a tile of lines of length N in shared memory as [position][line]
+// (8 rows for X, 16 lines for Y, 2 x 8 for Z; lines fastest, so every warp access covers whole
+// rows), issue all of a thread's global loads before storing any, transform in place
+// (dif_lines) and read the kept frequencies at their digit-reversed positions.
 constexpr int kPassLines = 16;
 
 template <int N>
