@@ -281,12 +281,17 @@ class SqomJob:
         self._copy_stream = None
         self._d2h_stream = None      # output copies to host torch tensors
         self._d2h_done = None
+        self._pending_out = []       # (device buffer, host tensor, ready event) not yet issued
         self._stage = {}             # device staging buffers of those outputs
         check(L.mpsq_job_create(C.byref(d), C.c_void_p(stream or 0), C.byref(self._h)), "job_create")
 
     # ------------------------------------------------------------------ lifecycle
     def close(self):
         if self._h:
+            if self._pending_out:            # owed copies of outputs to host tensors
+                self._flush_outputs()
+            if self._d2h_done is not None:
+                self._d2h_done.synchronize()
             _lib.load().mpsq_job_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -372,6 +377,8 @@ class SqomJob:
             ev.record(cs)
             job_stream.wait_event(ev)
             self.transform(c0, n)
+        # copies of earlier outputs to the host go after the uploads, on the same stream
+        self._flush_outputs(cs)
         self._keep = frames
 
     def transform(self, first: int = 0, count: int | None = None):
@@ -393,9 +400,10 @@ class SqomJob:
             float(g.q_min[1]), C.c_void_p(base.ctypes.data)), "transform_onephonon")
 
     def sync(self):
+        self._flush_outputs()
         check(_lib.load().mpsq_job_sync(self._h), "sync")
-        if self._d2h_stream is not None:
-            self._d2h_stream.synchronize()
+        if self._d2h_done is not None:
+            self._d2h_done.synchronize()
 
     def _torch_stream(self):
         import torch
@@ -404,9 +412,10 @@ class SqomJob:
     def _target(self, out, key, shape):
         """Where an output is computed: (pointer, host flag for the C call, host torch tensor
         to copy to afterwards or None).  A host torch tensor (pinned for a real overlap) is
-        filled from a device staging buffer by an asynchronous copy on a separate stream, so
-        that the copy overlaps whatever the job's stream runs next; sync() or wait_outputs()
-        orders it."""
+        filled from a device staging buffer by an asynchronous copy on another stream that
+        overlaps whatever the job's stream runs next.  The copy is issued by the next
+        transform_from_host after its uploads (so that the two directions do not share the
+        host link while the transform waits for its frames), or by sync() / wait_outputs()."""
         if out is None or not hasattr(out, "is_cuda"):
             return out, 1, None
         if out.is_cuda:
@@ -416,25 +425,39 @@ class SqomJob:
         if dev is None or tuple(dev.shape) != tuple(shape):
             dev = torch.empty(shape, dtype=torch.float32, device="cuda")
             self._stage[key] = dev
+        if any(p[0].data_ptr() == dev.data_ptr() for p in self._pending_out):
+            self._flush_outputs()               # the buffer's earlier content is still owed
         if self._d2h_done is not None:          # the previous copy out of the buffer
             self._torch_stream().wait_event(self._d2h_done)
         return dev, 0, out
 
     def _copy_out(self, dev, host):
         import torch
-        if self._d2h_stream is None:
-            self._d2h_stream = torch.cuda.Stream()
         ready = torch.cuda.Event()
         ready.record(self._torch_stream())
-        self._d2h_stream.wait_event(ready)
-        with torch.cuda.stream(self._d2h_stream):
-            host.copy_(dev.view(host.shape), non_blocking=True)
+        self._pending_out.append((dev, host, ready))
+
+    def _flush_outputs(self, stream=None):
+        """Issues the owed output copies on `stream` (default: the job's output stream)."""
+        if not self._pending_out:
+            return
+        import torch
+        if stream is None:
+            if self._d2h_stream is None:
+                self._d2h_stream = torch.cuda.Stream()
+            stream = self._d2h_stream
+        with torch.cuda.stream(stream):
+            for dev, host, ready in self._pending_out:
+                stream.wait_event(ready)
+                host.copy_(dev.view(host.shape), non_blocking=True)
+        self._pending_out = []
         self._d2h_done = torch.cuda.Event()
-        self._d2h_done.record(self._d2h_stream)
+        self._d2h_done.record(stream)
 
     def wait_outputs(self):
-        """Makes the job's stream wait, on the device, for the pending copies of outputs to
-        host tensors (no host synchronisation)."""
+        """Issues the owed copies of outputs to host tensors and makes the job's stream wait
+        for them, on the device (no host synchronisation)."""
+        self._flush_outputs()
         if self._d2h_done is not None:
             self._torch_stream().wait_event(self._d2h_done)
 
