@@ -33,3 +33,25 @@ def test_library_exports_all_declared(lib):
 def test_version_and_counters(lib):
     assert b"sm_103a" in lib.mpsq_version()
     assert lib.mpsq_launch_count() >= 0
+
+
+def _c_struct_members():
+    text = (ROOT / "include" / "mpsq.h").read_text()
+    body = text[text.index("typedef struct mpsq_job_desc {"):text.index("} mpsq_job_desc;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    return re.findall(r"^\s*(?:int32_t|int64_t|double)\s+([a-z_0-9]+)", body, flags=re.M)
+
+
+def test_job_descriptor_bindings_match_the_header():
+    """The ctypes mirror and the Fortran bind(C) type list the C struct's members in order."""
+    from mp_tools_gb300 import _lib
+    members = _c_struct_members()
+    assert members[0] == "ndim" and members[-1] == "stream_ordered"
+    assert [f[0] for f in _lib.JobDesc._fields_] == members
+    f90 = (ROOT / "include" / "mpsq_api.f90").read_text()
+    typ = f90[f90.index("type, bind(C), public :: mpsq_job_desc_t"):f90.index("end type")]
+    fnames = re.findall(r"::\s*([a-z_0-9]+)", typ)[1:]      # skip the type name itself
+    assert fnames == members
+    # every function the Fortran module binds is exported under that name
+    bound = set(re.findall(r'bind\(C, name="([a-z_0-9]+)"\)', f90))
+    assert bound and bound <= set(header_functions())
