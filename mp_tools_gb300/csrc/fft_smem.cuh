@@ -289,10 +289,10 @@ struct DifNoPre {
   __device__ __forceinline__ void operator()(float2 (&)[R], int, int, int) const {}
 };
 
-template <int N, int L, int S, int P, class Pre>
+template <int N, int L, int S, int P, int SE, class Pre>
 __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
                                                const float2* __restrict__ tw, const Pre& pre) {
-  if constexpr (S < dif_stages(N, P)) {
+  if constexpr (S < SE) {
     constexpr int r = dif_radix(N, S, P);
     constexpr int B = dif_block(N, S, P);
     constexpr int M = B / r;
@@ -314,7 +314,7 @@ __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
         for (int k = 0; k < r; ++k) xs[(base + M * k) * L + ln] = va[k];
       }
       __syncthreads();
-      dif_lines_from<N, L, S + 1, P>(xs, tw, pre);
+      dif_lines_from<N, L, S + 1, P, SE>(xs, tw, pre);
       return;
     }
     constexpr int LP = L / 2;      // a thread transforms two adjacent lines (16-byte accesses)
@@ -348,7 +348,7 @@ __device__ __forceinline__ void dif_lines_from(float2* __restrict__ xs,
             make_float4(va[k].x, va[k].y, vb[k].x, vb[k].y);
     }
     __syncthreads();
-    dif_lines_from<N, L, S + 1, P>(xs, tw, pre);
+    dif_lines_from<N, L, S + 1, P, SE>(xs, tw, pre);
   }
 }
 // L must be even; xs must be 16-byte aligned.
@@ -356,7 +356,15 @@ template <int N, int L, class Pre = DifNoPre, int P = kDifTwoStage>
 __device__ __forceinline__ void dif_lines(float2* __restrict__ xs, const float2* __restrict__ tw,
                                           const Pre& pre = Pre()) {
   static_assert(L % 2 == 0, "dif_lines transforms lines in pairs");
-  dif_lines_from<N, L, 0, P>(xs, tw, pre);
+  dif_lines_from<N, L, 0, P, dif_stages(N, P)>(xs, tw, pre);
+}
+// The first SE stages only (a caller that finishes the last stage in registers).
+template <int N, int L, int SE, class Pre = DifNoPre, int P = kDifTwoStage>
+__device__ __forceinline__ void dif_lines_until(float2* __restrict__ xs,
+                                                const float2* __restrict__ tw,
+                                                const Pre& pre = Pre()) {
+  static_assert(L % 2 == 0, "dif_lines transforms lines in pairs");
+  dif_lines_from<N, L, 0, P, SE>(xs, tw, pre);
 }
 
 // tw[n] = exp(-2 pi i n / N), n < N (all threads of the block; no barrier).

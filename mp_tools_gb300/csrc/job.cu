@@ -666,23 +666,44 @@ __global__ void __launch_bounds__(16 * L, (N <= 512 ? 48 / L : 1))
     }
   }
   __syncthreads();
-  dif_lines<N, L>(xs, tw);
-  float4 o[OUTS];
+  constexpr int NS = dif_stages(N), RL = dif_radix(N, NS - 1);
+  if constexpr (NS == 2 && RL > 8 && L * (N / RL) == NT) {
+    // two-stage plan: the last stage (contiguous groups of RL, no twiddles) is finished in
+    // registers, one (line, group) per thread, and only the kept frequencies are written,
+    // straight into the [row][K0] staging layout; output k of group gi is frequency
+    // gi + (N / RL) k
+    dif_lines_until<N, L, NS - 1>(xs, tw);
+    const int ln = tid % L, gi = tid / L;
+    float2 v[RL];
 #pragma unroll
-  for (int p = 0; p < OUTS; ++p) {
-    const int e = tid + NT * p;
-    o[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (e < LP * K0)
-      o[p] = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(e / LP - h0, N)) * L + 2 * (e % LP)]);
-  }
-  __syncthreads();
+    for (int k = 0; k < RL; ++k) v[k] = xs[(gi * RL + k) * L + ln];
+    dft_r(v, RL);
+    __syncthreads();                     // every input has been read
 #pragma unroll
-  for (int p = 0; p < OUTS; ++p) {
-    const int e = tid + NT * p;
-    if (e < LP * K0) {
-      const int r = 2 * (e % LP), i = e / LP;
-      xs[r * K0 + i] = make_float2(o[p].x, o[p].y);
-      xs[(r + 1) * K0 + i] = make_float2(o[p].z, o[p].w);
+    for (int k = 0; k < RL; ++k) {
+      const int f = gi + (N / RL) * k;
+      const int i = f <= h0 ? f + h0 : (f >= N - h0 ? f - N + h0 : -1);
+      if (i >= 0 && i < K0) xs[ln * K0 + i] = v[k];
+    }
+  } else {
+    dif_lines<N, L>(xs, tw);
+    float4 o[OUTS];
+#pragma unroll
+    for (int p = 0; p < OUTS; ++p) {
+      const int e = tid + NT * p;
+      o[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (e < LP * K0)
+        o[p] = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(e / LP - h0, N)) * L + 2 * (e % LP)]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < OUTS; ++p) {
+      const int e = tid + NT * p;
+      if (e < LP * K0) {
+        const int r = 2 * (e % LP), i = e / LP;
+        xs[r * K0 + i] = make_float2(o[p].x, o[p].y);
+        xs[(r + 1) * K0 + i] = make_float2(o[p].z, o[p].w);
+      }
     }
   }
   __syncthreads();

@@ -218,3 +218,29 @@ def test_outputs_to_host_tensors_are_copied_asynchronously(cuda):
         assert rel_l2(host_sq.numpy(), dev_sq.cpu().numpy()) < 1e-5
     finally:
         job.close()
+
+
+@pytest.mark.parametrize("q_range,box", [(2.95, 100.0), (3.96, 100.0), (5.97, 100.0)])
+def test_pruned_passes_match_cufft_path(cuda, q_range, box):
+    """The pruned three-pass transform (two-stage radix plans, last stage finished in
+    registers for the X pass) against cuFFT + the separate deconvolution, on fine grids of
+    192, 256 and 384 points (95^3, 127^3, 191^3 modes; packed Al/U pair, X-ray weights)."""
+    rng = np.random.default_rng(int(box))
+    n = 20000
+    fr = np.zeros((2, n, 4), np.float32)
+    fr[:, :, :3] = rng.uniform(-box / 2, box / 2, (n, 3)).astype(np.float32)
+    fr[1, :, :3] += rng.normal(0, 0.3, (n, 3)).astype(np.float32)
+    counts = [18400, 1600]
+    grid = sql.SqlGrid(q_range, (box,) * 3)
+    kw = dict(species_counts=counts, n_frames=2, precision=_lib.FP32, eps=1e-6,
+              n_atoms_frame=n, weight_mode=_lib.WEIGHT_XRAY, xff=[XFF_AL, XFF_U])
+    out = {}
+    for pruned in (True, False):
+        job = SqomJob(grid, no_pruned_fft=not pruned, **kw)
+        try:
+            job.set_frames(fr)
+            job.transform()
+            out[pruned] = job.amplitudes()
+        finally:
+            job.close()
+    assert rel_l2(out[True], out[False]) < 2e-6, grid.n_q
