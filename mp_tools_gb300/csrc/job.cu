@@ -747,16 +747,38 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     }
   }
   __syncthreads();
-  dif_lines<N, L>(xs, tw);
   float2* dst = b2 + ((int64_t)g * n2 + z) * (int64_t)K1 * K0;
-  for (int e = tid; e < LP * K1; e += 256) {
-    const int c = 2 * (e % LP), i = e / LP;
-    const int x = x0 + c;
-    if (x >= K0) continue;
-    const float4 v = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(i - h1, N)) * L + c]);
-    float2* q = dst + (int64_t)i * K0 + x;
-    q[0] = make_float2(v.x, v.y);
-    if (x + 1 < K0) q[1] = make_float2(v.z, v.w);
+  constexpr int NS = dif_stages(N), RL = dif_radix(N, NS - 1);
+  if constexpr (NS == 2 && RL > 8 && L * (N / RL) == 256) {
+    // two-stage plan: the last stage is finished in registers, one (column, group) per
+    // thread, and the kept frequencies go straight to b2 (the 16 columns of a group are
+    // contiguous); output k of group gi is frequency gi + (N / RL) k
+    dif_lines_until<N, L, NS - 1>(xs, tw);
+    const int ln = tid % L, gi = tid / L;
+    float2 v[RL];
+#pragma unroll
+    for (int k = 0; k < RL; ++k) v[k] = xs[(gi * RL + k) * L + ln];
+    dft_r(v, RL);
+    const int x = x0 + ln;
+    if (x < K0) {
+#pragma unroll
+      for (int k = 0; k < RL; ++k) {
+        const int f = gi + (N / RL) * k;
+        const int i = f <= h1 ? f + h1 : (f >= N - h1 ? f - N + h1 : -1);
+        if (i >= 0 && i < K1) dst[(int64_t)i * K0 + x] = v[k];
+      }
+    }
+  } else {
+    dif_lines<N, L>(xs, tw);
+    for (int e = tid; e < LP * K1; e += 256) {
+      const int c = 2 * (e % LP), i = e / LP;
+      const int x = x0 + c;
+      if (x >= K0) continue;
+      const float4 v = *reinterpret_cast<const float4*>(&xs[dif_position<N>(wrap_freq(i - h1, N)) * L + c]);
+      float2* q = dst + (int64_t)i * K0 + x;
+      q[0] = make_float2(v.x, v.y);
+      if (x + 1 < K0) q[1] = make_float2(v.z, v.w);
+    }
   }
 }
 
