@@ -193,19 +193,22 @@ def cpu_port_frames(pos0, counts, box, grid, n_frames, rng_seed=SEED + 2):
     qz = origin[2] + k[2] * steps[2][2]
     q2 = (qz[:, None, None] ** 2 + qy[None, :, None] ** 2 + qx[None, None, :] ** 2)
     weights = [sqom_ref.xray_ff(synth.XFF[s], kappa * q2) for s in ("Al", "U")]
+    weights = [np.ascontiguousarray(wt.ravel(), dtype=np.float64) for wt in weights]
+    cs = np.empty(grid.n_modes, np.complex128)
+    s_q = np.zeros(grid.n_modes, np.float64)
+    axes = [grid.axis[a].astype(np.float64) * float(grid.tpe[a]) for a in range(3)]
     total_pts, elapsed = 0, 0.0
     for t in range(n_frames):
         if t > 0:
             p = p + rng.normal(0, SIGMA, p.shape).astype(np.float32)
             p = (np.remainder(p + half, box) - half).astype(np.float32)
         t0 = time.perf_counter()
-        cs = None
         for s in range(len(counts)):
             r = p[off[s]:off[s + 1]].astype(np.float64)
-            coords = [r @ grid.axis[a].astype(np.float64) * float(grid.tpe[a]) for a in range(3)]
+            coords = [r @ axes[a] for a in range(3)]
             A = oracle.es_nufft(coords, np.ones(len(r)), -1, EPS, grid.n_q)
-            cs = weights[s] * A if cs is None else cs + weights[s] * A
-        np.abs(cs) ** 2  # the |F|^2 accumulation of the frame
+            oracle.weight_accumulate(cs, weights[s], A, first=(s == 0))
+        oracle.abs2_accumulate(s_q, cs)   # the |F|^2 accumulation of the frame
         elapsed += time.perf_counter() - t0
         total_pts += int(off[-1])
     return elapsed, total_pts, oracle.num_threads()

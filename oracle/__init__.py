@@ -47,7 +47,7 @@ def build(force: bool = False) -> Path:
         return LIB
     BUILD.mkdir(parents=True, exist_ok=True)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", str(tmp), *map(str, SRC), "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", str(tmp), *map(str, SRC), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
@@ -65,6 +65,10 @@ def _load():
         lib.oracle_dirft3d1.argtypes = [i64, vp, vp, vp, vp, C.c_int, i64, i64, i64, vp]
         lib.oracle_dirft_modes.argtypes = [C.c_int, i64, vp, vp, vp, vp, C.c_int, i64, vp, vp]
         lib.oracle_es_spread.argtypes = [C.c_int, i64, vp, vp, C.c_int, C.c_double, i64, i64, i64, vp]
+        lib.oracle_zero.argtypes = [vp, i64]
+        lib.oracle_weight_accumulate.argtypes = [i64, vp, vp, vp, C.c_int]
+        lib.oracle_abs2_accumulate.argtypes = [i64, vp, vp]
+        lib.oracle_es_extract.argtypes = [C.c_int, vp, i64, i64, i64, i64, i64, i64, vp, vp, vp, vp]
         lib.oracle_num_threads.restype = C.c_int
         _lib = lib
     return _lib
@@ -148,6 +152,36 @@ def es_phihat(w, beta, nf, m):
     return (f[None, :] * np.cos(2 * np.pi * k[:, None] * u[None, :] / nf)).sum(axis=1)
 
 
+def weight_accumulate(cs, w, A, first):
+    """cs = (0 if first else cs) + w * A over the flattened Q grid, in place (complex128 cs and
+    A, float64 w; OpenMP)."""
+    assert cs.dtype == np.complex128 and cs.flags.c_contiguous and cs.size == A.size == w.size
+    A, w = _c128(A), _f64(w)
+    _load().oracle_weight_accumulate(cs.size, w.ctypes.data, A.ctypes.data, cs.ctypes.data,
+                                     int(bool(first)))
+
+
+def abs2_accumulate(s, cs):
+    """s += |cs|^2 in place (float64 s, complex128 cs; OpenMP)."""
+    assert s.dtype == np.float64 and s.flags.c_contiguous and s.size == cs.size
+    cs = _c128(cs)
+    _load().oracle_abs2_accumulate(s.size, cs.ctypes.data, s.ctypes.data)
+
+
+_grid_cache = None
+
+
+def _fine_grid(shape):
+    """A zeroed complex128 fine grid; the buffer of the previous call of the same shape is
+    reused (zeroed in parallel in C), as a plan reuses its grid across repeated transforms."""
+    global _grid_cache
+    if _grid_cache is None or _grid_cache.shape != shape:
+        _grid_cache = None
+        _grid_cache = np.empty(shape, np.complex128)
+    _load().oracle_zero(_grid_cache.ctypes.data, 2 * _grid_cache.size)
+    return _grid_cache
+
+
 def es_nufft(coords, c, iflag, eps, modes, workers=None):
     """CPU type-1 NUFFT (FP64).  coords: list of 2 or 3 coordinate arrays (radians);
     modes: (m1, m2[, m3]).  Returns complex128 of shape modes[::-1] (k1 fastest)."""
@@ -165,22 +199,20 @@ def es_nufft(coords, c, iflag, eps, modes, workers=None):
         g[:, d] = gd
     c = _c128(c)
     shape = (nf[2] if dim == 3 else 1, nf[1], nf[0])
-    grid = np.zeros(shape, np.complex128)
+    grid = _fine_grid(shape)
     _load().oracle_es_spread(dim, nj, g.ctypes.data, c.ctypes.data, w, beta, nf[0], nf[1],
                              nf[2] if dim == 3 else 1, grid.ctypes.data)
     axes = tuple(range(3 - dim, 3))
     workers = workers or num_threads()
     if iflag >= 0:
-        G = scipy.fft.ifftn(grid, axes=axes, workers=workers, overwrite_x=True) * np.prod(nf)
+        G = scipy.fft.ifftn(grid, axes=axes, workers=workers, overwrite_x=True, norm="forward")
     else:
         G = scipy.fft.fftn(grid, axes=axes, workers=workers, overwrite_x=True)
-    if dim == 2:
-        G = G[0]
-    idx = [(np.arange(m) - m // 2) % n for m, n in zip(modes, nf)]
-    corr = [1.0 / es_phihat(w, beta, n, m) for m, n in zip(modes, nf)]
-    if dim == 2:
-        out = G[np.ix_(idx[1], idx[0])] * corr[1][:, None] * corr[0][None, :]
-    else:
-        out = G[np.ix_(idx[2], idx[1], idx[0])] * (corr[2][:, None, None] * corr[1][None, :, None]
-                                                   * corr[0][None, None, :])
+    corr = [np.ascontiguousarray(1.0 / es_phihat(w, beta, n, m)) for m, n in zip(modes, nf)]
+    G = np.ascontiguousarray(G, dtype=np.complex128)
+    out = np.empty(tuple(modes[::-1]), np.complex128)
+    m = list(modes) + [1] * (3 - dim)
+    _load().oracle_es_extract(dim, G.ctypes.data, nf[0], nf[1], nf[2] if dim == 3 else 1, m[0],
+                              m[1], m[2], corr[0].ctypes.data, corr[1].ctypes.data,
+                              corr[2].ctypes.data if dim == 3 else None, out.ctypes.data)
     return out

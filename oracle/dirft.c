@@ -120,12 +120,60 @@ void oracle_dirft_modes(int dim, int64_t nj, const double* x, const double* y, c
 
 /* CPU exponential-of-semicircle spreading onto an n0 x n1 x n2 periodic grid (interleaved
  * complex, x fastest, zeroed by the caller).  g: 3*nj grid coordinates already folded to
- * [0, n).  Threads own disjoint z-planes (y-rows in 2D, n2 == 1), so no two threads write the
- * same cell.  Kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)) on w cells. */
+ * [0, n).  Kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)) on w cells per axis.
+ *
+ * Organisation (the sorted, block-wise spreading of Barnett, Magland, af Klinteberg 2019, sec. 3):
+ * the points are counting-sorted by the 8^dim block of their first support cell, slowest along
+ * the partitioned axis (z in 3D, y in 2D); each thread owns a contiguous range of planes (rows)
+ * of that axis and walks only the blocks whose support reaches them, so no two threads write
+ * the same cell and consecutive points touch neighbouring grid memory.  Each point's wrapped
+ * support indices are formed once; a support that does not wrap along x is one contiguous run
+ * of the row.  Contributions to a cell are summed in the sorted point order. */
+#define ES_BLOCK 8
+#define ES_WMAX 32
+
+static inline int64_t wrap_index(int64_t i, int64_t n) {
+  int64_t r = i % n;
+  return r < 0 ? r + n : r;
+}
+
 void oracle_es_spread(int dim, int64_t nj, const double* g, const double* c, int w, double beta,
                       int64_t n0, int64_t n1, int64_t n2, double* grid) {
-  const int64_t nslab = dim == 3 ? n2 : n1; /* partitioned axis */
-  const int ax = dim == 3 ? 2 : 1;
+  if (nj <= 0 || w < 1 || w > ES_WMAX) return;
+  const int ax = dim == 3 ? 2 : 1;                      /* partitioned axis */
+  const int64_t nslab = dim == 3 ? n2 : n1;
+  const int64_t nb0 = (n0 + ES_BLOCK - 1) / ES_BLOCK, nb1 = (n1 + ES_BLOCK - 1) / ES_BLOCK;
+  const int64_t nb2 = dim == 3 ? (n2 + ES_BLOCK - 1) / ES_BLOCK : 1;
+  const int64_t nkeys = nb0 * nb1 * nb2;
+  const int64_t nbs = dim == 3 ? nb2 : nb1;             /* blocks along the partitioned axis */
+  const int64_t per_slab_block = nkeys / nbs;           /* keys per block of that axis */
+  int64_t* start = (int64_t*)malloc(3 * sizeof(int64_t) * (size_t)nj);   /* wrapped first cells */
+  int64_t* key = (int64_t*)malloc(sizeof(int64_t) * (size_t)nj);
+  int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (size_t)nj);
+  int64_t* off = (int64_t*)calloc((size_t)nkeys + 1, sizeof(int64_t));
+  if (!start || !key || !order || !off) {
+    free(start); free(key); free(order); free(off);
+    return;
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < nj; ++j) {
+    const double* gj = g + 3 * j;
+    int64_t s0 = wrap_index((int64_t)ceil(gj[0] - 0.5 * w), n0);
+    int64_t s1 = wrap_index((int64_t)ceil(gj[1] - 0.5 * w), n1);
+    int64_t s2 = dim == 3 ? wrap_index((int64_t)ceil(gj[2] - 0.5 * w), n2) : 0;
+    start[3 * j] = s0; start[3 * j + 1] = s1; start[3 * j + 2] = s2;
+    key[j] = ((s2 / ES_BLOCK) * nb1 + s1 / ES_BLOCK) * nb0 + s0 / ES_BLOCK;
+  }
+  /* stable counting sort of the points by key */
+  for (int64_t j = 0; j < nj; ++j) off[key[j] + 1]++;
+  for (int64_t k = 0; k < nkeys; ++k) off[k + 1] += off[k];
+  {
+    int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * (size_t)nkeys);
+    if (!cur) { free(start); free(key); free(order); free(off); return; }
+    memcpy(cur, off, sizeof(int64_t) * (size_t)nkeys);
+    for (int64_t j = 0; j < nj; ++j) order[cur[key[j]]++] = j;
+    free(cur);
+  }
 #pragma omp parallel
   {
     int nt = 1, tid = 0;
@@ -134,48 +182,122 @@ void oracle_es_spread(int dim, int64_t nj, const double* g, const double* c, int
     tid = omp_get_thread_num();
 #endif
     const int64_t lo = nslab * tid / nt, hi = nslab * (tid + 1) / nt;
-    double kx[32], ky[32], kz[32];
-    for (int64_t j = 0; j < nj; ++j) {
-      const double* gj = g + 3 * j;
-      int64_t i0[3];
-      for (int d = 0; d < 3; ++d) i0[d] = (int64_t)ceil(gj[d] - 0.5 * w);
-      /* does the support along the partitioned axis meet [lo, hi) (periodically)? */
-      int hit = 0;
-      for (int a = 0; a < w && !hit; ++a) {
-        int64_t cidx = (i0[ax] + a) % nslab;
-        if (cidx < 0) cidx += nslab;
-        if (cidx >= lo && cidx < hi) hit = 1;
+    double kx[ES_WMAX], ky[ES_WMAX], kz[ES_WMAX];
+    int64_t ix[ES_WMAX], iy[ES_WMAX], iz[ES_WMAX];
+    const double inv = 2.0 / w;
+    for (int64_t bs = 0; bs < nbs && lo < hi; ++bs) {
+      /* support planes of this block: [bs*B, min(bs*B + B, nslab) + w - 1), periodically */
+      const int64_t first = bs * ES_BLOCK;
+      const int64_t span = (first + ES_BLOCK < nslab ? ES_BLOCK : nslab - first) + w - 1;
+      int meets = 0;
+      if (span >= nslab) {
+        meets = 1;
+      } else {
+        for (int64_t p = 0; p < span && !meets; ++p) {
+          const int64_t q = (first + p) % nslab;
+          if (q >= lo && q < hi) meets = 1;
+        }
       }
-      if (!hit) continue;
-      for (int a = 0; a < w; ++a) {
-        double zx = ((double)(i0[0] + a) - gj[0]) * 2.0 / w;
-        double zy = ((double)(i0[1] + a) - gj[1]) * 2.0 / w;
-        double zz = ((double)(i0[2] + a) - gj[2]) * 2.0 / w;
-        kx[a] = exp(beta * (sqrt(fmax(0.0, 1.0 - zx * zx)) - 1.0));
-        ky[a] = exp(beta * (sqrt(fmax(0.0, 1.0 - zy * zy)) - 1.0));
-        kz[a] = dim == 3 ? exp(beta * (sqrt(fmax(0.0, 1.0 - zz * zz)) - 1.0)) : 1.0;
-      }
-      const int wz = dim == 3 ? w : 1;
-      for (int az = 0; az < wz; ++az) {
-        int64_t iz = dim == 3 ? (i0[2] + az) % n2 : 0;
-        if (iz < 0) iz += n2;
-        if (dim == 3 && (iz < lo || iz >= hi)) continue;
-        for (int ay = 0; ay < w; ++ay) {
-          int64_t iy = (i0[1] + ay) % n1;
-          if (iy < 0) iy += n1;
-          if (dim == 2 && (iy < lo || iy >= hi)) continue;
-          const double v = kz[az] * ky[ay];
-          const double vr = v * c[2 * j], vi = v * c[2 * j + 1];
-          double* row = grid + 2 * ((iz * n1 + iy) * n0);
-          for (int axx = 0; axx < w; ++axx) {
-            int64_t ix = (i0[0] + axx) % n0;
-            if (ix < 0) ix += n0;
-            row[2 * ix] += vr * kx[axx];
-            row[2 * ix + 1] += vi * kx[axx];
+      if (!meets) continue;
+      const int64_t e0 = off[bs * per_slab_block], e1 = off[(bs + 1) * per_slab_block];
+      for (int64_t e = e0; e < e1; ++e) {
+        const int64_t j = order[e];
+        const double* gj = g + 3 * j;
+        const int64_t* sj = start + 3 * j;
+        /* the unwrapped first cell: the wrapped one minus a multiple of n, so the offsets to
+         * the point are the same */
+        const double f0 = ceil(gj[0] - 0.5 * w), f1 = ceil(gj[1] - 0.5 * w);
+        const double f2 = dim == 3 ? ceil(gj[2] - 0.5 * w) : 0.0;
+        for (int a = 0; a < w; ++a) {
+          const double zx = (f0 + a - gj[0]) * inv, zy = (f1 + a - gj[1]) * inv;
+          kx[a] = exp(beta * (sqrt(fmax(0.0, 1.0 - zx * zx)) - 1.0));
+          ky[a] = exp(beta * (sqrt(fmax(0.0, 1.0 - zy * zy)) - 1.0));
+          if (dim == 3) {
+            const double zz = (f2 + a - gj[2]) * inv;
+            kz[a] = exp(beta * (sqrt(fmax(0.0, 1.0 - zz * zz)) - 1.0));
+          } else {
+            kz[a] = 1.0;
+          }
+          int64_t t = sj[0] + a; ix[a] = t >= n0 ? t - n0 : t;
+          t = sj[1] + a; iy[a] = t >= n1 ? t - n1 : t;
+          t = sj[2] + a; iz[a] = dim == 3 ? (t >= n2 ? t - n2 : t) : 0;
+        }
+        const int contiguous = sj[0] + w <= n0;
+        const double cr = c[2 * j], ci = c[2 * j + 1];
+        const int wz = dim == 3 ? w : 1;
+        for (int az = 0; az < wz; ++az) {
+          if (dim == 3 && (iz[az] < lo || iz[az] >= hi)) continue;
+          for (int ay = 0; ay < w; ++ay) {
+            if (dim == 2 && (iy[ay] < lo || iy[ay] >= hi)) continue;
+            const double v = kz[az] * ky[ay];
+            const double vr = v * cr, vi = v * ci;
+            double* row = grid + 2 * ((iz[az] * n1 + iy[ay]) * n0);
+            if (contiguous) {
+              double* cell = row + 2 * sj[0];
+              for (int a = 0; a < w; ++a) {
+                cell[2 * a] += vr * kx[a];
+                cell[2 * a + 1] += vi * kx[a];
+              }
+            } else {
+              for (int a = 0; a < w; ++a) {
+                row[2 * ix[a]] += vr * kx[a];
+                row[2 * ix[a] + 1] += vi * kx[a];
+              }
+            }
           }
         }
       }
     }
+  }
+  free(start); free(key); free(order); free(off);
+}
+
+/* Deconvolution and mode extraction of the type-1 NUFFT: out[k2][k1][k0] = G[(k2 - m2/2) mod n2]
+ * [(k1 - m1/2) mod n1][(k0 - m0/2) mod n0] * c0[k0] c1[k1] c2[k2] (interleaved complex, k0
+ * fastest; dim 2: m2 = n2 = 1 and c2 unused). */
+void oracle_es_extract(int dim, const double* G, int64_t n0, int64_t n1, int64_t n2, int64_t m0,
+                       int64_t m1, int64_t m2, const double* c0, const double* c1,
+                       const double* c2, double* out) {
+  if (dim != 3) { m2 = 1; n2 = 1; }
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < m2 * m1; ++r) {
+    const int64_t k2 = r / m1, k1 = r % m1;
+    const int64_t i2 = wrap_index(k2 - m2 / 2, n2), i1 = wrap_index(k1 - m1 / 2, n1);
+    const double f = c1[k1] * (dim == 3 ? c2[k2] : 1.0);
+    const double* src = G + 2 * ((i2 * n1 + i1) * n0);
+    double* dst = out + 2 * r * m0;
+    for (int64_t k0 = 0; k0 < m0; ++k0) {
+      const int64_t i0 = wrap_index(k0 - m0 / 2, n0);
+      const double t = f * c0[k0];
+      dst[2 * k0] = src[2 * i0] * t;
+      dst[2 * k0 + 1] = src[2 * i0 + 1] * t;
+    }
+  }
+}
+
+/* Species weighting of one frame: cs[i] = (first ? 0 : cs[i]) + w[i] A[i] (A, cs interleaved
+ * complex, w real per Q), the sum over species of code/src/mp_sqom56.f90:1338-1377. */
+void oracle_weight_accumulate(int64_t n, const double* w, const double* A, double* cs, int first) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const double re = w[i] * A[2 * i], im = w[i] * A[2 * i + 1];
+    cs[2 * i] = first ? re : cs[2 * i] + re;
+    cs[2 * i + 1] = first ? im : cs[2 * i + 1] + im;
+  }
+}
+
+/* |F|^2 accumulation over frames: s[i] += |cs[i]|^2 (code/src/mp_sqom56.f90:1381-1387). */
+void oracle_abs2_accumulate(int64_t n, const double* cs, double* s) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) s[i] += cs[2 * i] * cs[2 * i] + cs[2 * i + 1] * cs[2 * i + 1];
+}
+
+/* Parallel zeroing of n doubles (also the first touch of a fresh buffer's pages). */
+void oracle_zero(double* p, int64_t n) {
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < (n + 65535) / 65536; ++b) {
+    const int64_t i0 = b * 65536, m = n - i0 < 65536 ? n - i0 : 65536;
+    memset(p + i0, 0, sizeof(double) * (size_t)m);
   }
 }
 

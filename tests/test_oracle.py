@@ -78,6 +78,35 @@ def test_cpu_nufft_port_3d():
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-8
 
 
+@pytest.mark.parametrize("modes", [(5, 3, 4), (2, 2, 2), (33, 1, 7)])
+def test_cpu_nufft_port_small_grids(modes):
+    """Fine grids narrower than a sorting block plus the kernel width, and points on the
+    periodic edges: every block's support reaches every thread's planes."""
+    rng = np.random.default_rng(8)
+    n = 500
+    x, y, z = rng.uniform(-np.pi, np.pi, (3, n))
+    x[:4] = [-np.pi, np.pi - 1e-12, 0.0, -1e-15]
+    c = rng.normal(size=n) + 1j * rng.normal(size=n)
+    ref = oracle.dirft3d1(x, y, z, c, -1, *modes)
+    got = oracle.es_nufft([x, y, z], c, -1, 1e-9, modes)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_weighting_helpers_match_numpy():
+    """The CPU baseline's species weighting and |F|^2 accumulation (OpenMP loops)."""
+    rng = np.random.default_rng(9)
+    n = 1001
+    a, b = rng.normal(size=(2, n)) + 1j * rng.normal(size=(2, n))
+    w1, w2 = rng.normal(size=(2, n))
+    cs = np.empty(n, np.complex128)
+    oracle.weight_accumulate(cs, w1, a, first=True)
+    oracle.weight_accumulate(cs, w2, b, first=False)
+    assert np.array_equal(cs, w1 * a + w2 * b)
+    s = np.ones(n)
+    oracle.abs2_accumulate(s, cs)
+    assert np.allclose(s, 1.0 + np.abs(cs) ** 2, rtol=1e-15, atol=0)
+
+
 def test_dirft_modes_matches_full_sum():
     rng = np.random.default_rng(7)
     x, y, z = rng.uniform(-np.pi, np.pi, (3, 300))
