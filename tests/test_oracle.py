@@ -1,4 +1,7 @@
 """Oracle self-checks against known answers (CPU only)."""
+import os
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -90,6 +93,30 @@ def test_cpu_nufft_port_small_grids(modes):
     ref = oracle.dirft3d1(x, y, z, c, -1, *modes)
     got = oracle.es_nufft([x, y, z], c, -1, 1e-9, modes)
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_cpu_nufft_port_independent_of_thread_count():
+    """Each cell is summed in the sorted point order by the one thread owning its plane, so
+    the port gives the same bits with 1 thread and with several."""
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, oracle\n"
+        "rng = np.random.default_rng(10)\n"
+        "x, y, z = rng.uniform(-np.pi, np.pi, (3, 4000))\n"
+        "c = rng.normal(size=4000) + 1j * rng.normal(size=4000)\n"
+        "f = oracle.es_nufft([x, y, z], c, -1, 1e-6, (12, 10, 8))\n"
+        "g = oracle.es_nufft([x, y], c, 1, 1e-6, (20, 14))\n"
+        "import sys; sys.stdout.write(np.concatenate([f.ravel(), g.ravel()]).tobytes().hex())\n")
+    root = str(Path(__file__).resolve().parents[1])
+    outs = []
+    for n in ("1", "3"):
+        env = dict(os.environ, OMP_NUM_THREADS=n, PYTHONPATH=root)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                           cwd=root, timeout=120)
+        assert r.returncode == 0, r.stderr
+        outs.append(r.stdout)
+    assert outs[0] == outs[1]
 
 
 def test_weighting_helpers_match_numpy():
