@@ -307,7 +307,8 @@ def error_metrics(got, ref):
     strong = s_ref > 1e-3 * s_ref.max()
     return {"rel_l2_amplitude": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
             "rel_l2_S": float(np.linalg.norm(s_got - s_ref) / np.linalg.norm(s_ref)),
-            "max_rel_S": float(np.max(np.abs(s_got[strong] - s_ref[strong]) / s_ref[strong]))}
+            "max_rel_S": (float(np.max(np.abs(s_got[strong] - s_ref[strong]) / s_ref[strong]))
+                          if strong.any() else None)}
 
 
 def run_gpu(args):
