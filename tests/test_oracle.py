@@ -193,3 +193,58 @@ def test_iqt_identities():
     a = sqom_ref.econst(cs, 5, w, 2)
     b = sqom_ref.econst(x, 5, w, 2, center=False)
     np.testing.assert_allclose(a, b, rtol=1e-12)
+
+
+def test_hann_leakage_pattern_of_a_pure_tone():
+    """E=const map of a pure tone exp(2 pi i k0 t / n_int): every start frame contributes the
+    same |X|^2, so bin f holds n0 |H(f - 1 - k0)|^2 with H the DFT of the reference's Hann
+    window; the main lobe sits at bin k0 + 1 and the first neighbours carry about a quarter of
+    it (the symmetric window's -6 dB points), the far bins much less."""
+    n_int, k0 = 65, 5
+    F = 130                                   # ten whole periods: the elastic mean is zero
+    t = np.arange(F)
+    cs = np.exp(2j * np.pi * k0 * t / n_int)[:, None] * np.ones((1, 2))
+    h = sqom_ref.hann_window(n_int)
+    H = np.fft.fft(h)
+    n0 = F - n_int + 1
+    maps = np.array([sqom_ref.econst(cs, n_int, h, f)[0] for f in range(1, n_int // 2 + 2)])
+    want = n0 * np.abs(H[(np.arange(n_int // 2 + 1) - k0) % n_int]) ** 2
+    np.testing.assert_allclose(maps, want, rtol=1e-9, atol=1e-9 * maps.max())
+    assert np.argmax(maps) == k0
+    assert 0.23 < maps[k0 + 1] / maps[k0] < 0.27 and 0.23 < maps[k0 - 1] / maps[k0] < 0.27
+    assert np.all(maps[k0 + 3:] < 1e-3 * maps[k0])
+
+
+def test_plane_wave_displacement_satellites():
+    """A longitudinal plane wave u(R, t) = A e cos(2 pi q.R - 2 pi nu t) on a simple cubic
+    lattice: to first order in A the amplitude at G - q is -pi i (Q.e) A N exp(+2 pi i nu t) and
+    at G + q the same with exp(-2 pi i nu t); elsewhere off the lattice it vanishes.  In the
+    E=const map at the bin of nu (mp_sqom's phase convention) G - q carries
+    n0 (sum h)^2 |pi (Q.e) A N|^2 and G + q nothing."""
+    n, A = 8, 0.002
+    n_int, k0 = 33, 3
+    F = 66                                     # 6 periods of 11 frames
+    nu = k0 / n_int
+    R = np.stack(np.meshgrid(*(np.arange(n) - n // 2,) * 3, indexing="ij"), -1).reshape(-1, 3)
+    N = len(R)
+    q = np.array([1.0 / n, 0.0, 0.0])
+    kq = np.array([[n - 1, 0, 0], [n + 1, 0, 0], [n, 0, 0], [n + 1, 1, 0]])  # G-q, G+q, G, off
+    amps = np.empty((F, len(kq)), np.complex128)
+    for t in range(F):
+        r = R.astype(np.float64).copy()
+        r[:, 0] += A * np.cos(2 * np.pi * (R @ q) - 2 * np.pi * nu * t)
+        x, y, z = (2 * np.pi * r / n).T
+        amps[t] = oracle.dirft_modes(x, y, z, np.ones(N), -1, kq)
+    tt = np.arange(F)
+    for col, sign in ((0, +1), (1, -1)):
+        Qe = kq[col, 0] / n
+        want = -np.pi * 1j * Qe * A * N * np.exp(sign * 2j * np.pi * nu * tt)
+        assert np.abs(amps[:, col] - want).max() < 2e-3 * abs(want[0])
+    assert np.abs(amps[:, 2] - N).max() < 1e-3 * N            # Bragg: constant to O(A^2)
+    assert np.abs(amps[:, 3]).max() < 1e-6 * N                 # off-lattice, no satellite
+    h = sqom_ref.hann_window(n_int)
+    m = sqom_ref.econst(amps, n_int, h, k0 + 1)
+    n0 = F - n_int + 1
+    lo = n0 * h.sum() ** 2 * (np.pi * (kq[0, 0] / n) * A * N) ** 2
+    assert abs(m[0] / lo - 1) < 5e-3
+    assert m[1] < 1e-4 * m[0] and m[3] < 1e-9 * m[0]
