@@ -211,10 +211,55 @@ def frame_file(data_dir, master: str, index: int | None) -> Path:
     return Path(data_dir) / f"{master}_n{tag}.dat"
 
 
-def read_trajectory(data_dir, master: str, first: int, last: int, step: int = 1):
+def resolve_t_step(sim_type: str, t_step_header: float, t_dump0: float, t_dump1: float | None,
+                   n_frames: int, prefer: str | None = None) -> float:
+    """Time step between the frames used, as mp_sqom settles it (mp_sqom56.f90:304-342): 0
+    for a simulation type other than TIMESTEP (unrelated snapshots); otherwise the t_dump
+    difference of the first two frames used (the header's t_step for a single frame).  Where
+    that difference and the header's t_step differ by more than 1 % of the latter and more
+    than one frame is used, the reference asks which to take: prefer='header' or 'dump'
+    answers, None raises ValueError naming both values."""
+    if str(sim_type).strip().upper() != "TIMESTEP":
+        return 0.0
+    if t_dump1 is None or n_frames < 2:
+        return float(t_step_header)
+    dump = float(t_dump1) - float(t_dump0)
+    if abs(dump - t_step_header) > 0.01 * abs(t_step_header):
+        if prefer == "header":
+            return float(t_step_header)
+        if prefer == "dump":
+            return dump
+        raise ValueError(f"t_step {t_step_header} of the data header does not match the t_dump "
+                         f"difference {dump}: pass t_step_prefer='header' or 'dump'")
+    return dump
+
+
+def resolve_atom_names(par_names, dat_names, prefer: str | None = None) -> list:
+    """Species names of the .par atoms section checked against the .dat header's at_name_out
+    (mp_sqom56.f90:435-443).  Equal lists pass.  At a mismatch the reference asks whether to
+    take the .dat names: prefer='dat' returns them, 'par' keeps the .par names, None raises
+    ValueError naming the first species that differs.  Lists of different lengths are an
+    error."""
+    par_names, dat_names = [str(x).strip() for x in par_names], [str(x).strip() for x in dat_names]
+    if len(par_names) != len(dat_names):
+        raise ValueError(f"{len(par_names)} species in the .par atoms section, "
+                         f"{len(dat_names)} in the .dat header")
+    for j, (a, b) in enumerate(zip(par_names, dat_names), start=1):
+        if a != b:
+            if prefer == "dat":
+                return dat_names
+            if prefer == "par":
+                return par_names
+            raise ValueError(f"species {j}: {a!r} in the .par file, {b!r} in the .dat header: "
+                             "pass prefer='dat' or 'par'")
+    return par_names
+
+
+def read_trajectory(data_dir, master: str, first: int, last: int, step: int = 1,
+                    t_step_prefer: str | None = None):
     """Reads frames first..last into (frames, n_tot, 4) float32 plus the first frame's header,
-    cell indices and the time step between frames (t_dump difference, as mp_sqom derives it
-    at :303-342)."""
+    cell indices and the time step between frames (``resolve_t_step`` on the first frame's
+    header and the t_dump of the first two frames read, as mp_sqom derives it at :303-342)."""
     idx = list(range(first, last + 1, step))
     f0 = read_dat(frame_file(data_dir, master, idx[0]))
     frames = np.empty((len(idx), f0.n_tot, 4), np.float32)
@@ -226,7 +271,9 @@ def read_trajectory(data_dir, master: str, first: int, last: int, step: int = 1)
             raise ValueError(f"frame {i}: {f.n_tot} atoms, frame {idx[0]}: {f0.n_tot}")
         frames[k] = f.at_pos
         t_dump.append(float(f.header.get("t_dump", 0.0)))
-    t_step = (t_dump[1] - t_dump[0]) if len(idx) > 1 else float(f0.header.get("t_step", 0.0))
+    t_step = resolve_t_step(f0.header.get("sim_type", ""), float(f0.header.get("t_step", 0.0)),
+                            t_dump[0], t_dump[1] if len(idx) > 1 else None, len(idx),
+                            prefer=t_step_prefer)
     return frames, f0, t_step
 
 

@@ -78,14 +78,47 @@ def test_dat_rejects_corrupt_files(tmp_path):
 def test_trajectory_naming_and_reading(tmp_path):
     f = io.read_dat(ALU_DAT)
     for i in (1, 2, 3):
-        g = io.DatFrame(header=dict(f.header, t_dump=0.01 * i), at_ind=f.at_ind,
-                        at_pos=f.at_pos + np.float32(i))
+        g = io.DatFrame(header=dict(f.header, sim_type="TIMESTEP", t_step=0.01, t_dump=0.01 * i),
+                        at_ind=f.at_ind, at_pos=f.at_pos + np.float32(i))
         io.write_dat(io.frame_file(tmp_path, "traj", i), g)
     assert io.frame_file(tmp_path, "traj", 12).name == "traj_n0012.dat"
     frames, f0, t_step = io.read_trajectory(tmp_path, "traj", 1, 3)
     assert frames.shape == (3, 30000, 4)
     assert np.array_equal(frames[2], f.at_pos + np.float32(3))
     assert t_step == pytest.approx(0.01)
+    # snapshots of another simulation type are unrelated in time: t_step 0
+    g = io.DatFrame(header=dict(f.header, sim_type="STATIC", t_dump=0.5), at_ind=f.at_ind,
+                    at_pos=f.at_pos)
+    io.write_dat(io.frame_file(tmp_path, "stat", 1), g)
+    io.write_dat(io.frame_file(tmp_path, "stat", 2), g)
+    assert io.read_trajectory(tmp_path, "stat", 1, 2)[2] == 0.0
+
+
+def test_t_step_mismatch_is_reported():
+    """mp_sqom asks which value to take when the header's t_step and the t_dump difference
+    differ by more than 1 %; here the caller answers or gets an error."""
+    assert io.resolve_t_step("TIMESTEP", 0.01, 1.0, 1.01, 5) == pytest.approx(0.01)
+    assert io.resolve_t_step("TIMESTEP", 0.01, 1.0, 1.01005, 5) == pytest.approx(0.01005)
+    with pytest.raises(ValueError, match="t_dump difference"):
+        io.resolve_t_step("TIMESTEP", 0.01, 1.0, 1.02, 5)
+    assert io.resolve_t_step("TIMESTEP", 0.01, 1.0, 1.02, 5, prefer="header") == 0.01
+    assert io.resolve_t_step("TIMESTEP", 0.01, 1.0, 1.02, 5, prefer="dump") == pytest.approx(0.02)
+    assert io.resolve_t_step("TIMESTEP", 0.01, 1.0, None, 1) == 0.01
+    assert io.resolve_t_step("timestep", 0.01, 1.0, 1.02, 1) == 0.01   # one frame: no check
+    assert io.resolve_t_step("STATIC", 0.01, 1.0, 1.02, 5) == 0.0
+
+
+def test_atom_names_par_against_dat():
+    p = io.read_par(GOLDEN / "alu" / "Al_U_large.par")
+    f = io.read_dat(ALU_DAT)
+    par = [a[1] for a in p["atoms"]]
+    assert io.resolve_atom_names(par, f.header["at_name_out"]) == ["Al", "U"]
+    with pytest.raises(ValueError, match="species 2"):
+        io.resolve_atom_names(["Al", "Zr"], ["Al", "U"])
+    assert io.resolve_atom_names(["Al", "Zr"], ["Al", "U"], prefer="dat") == ["Al", "U"]
+    assert io.resolve_atom_names(["Al", "Zr"], ["Al", "U"], prefer="par") == ["Al", "Zr"]
+    with pytest.raises(ValueError, match="species in the .par"):
+        io.resolve_atom_names(["Al"], ["Al", "U"], prefer="dat")
 
 
 def test_read_par_namelist_and_atoms():
