@@ -157,11 +157,23 @@ struct mpsq_job {
   float* oneph_base = nullptr;
   cufftHandle oneph_fft = 0;
   bool have_oneph_fft = false;
+  int n_alloc = 0;  // device allocations made so far (fault injection below)
 };
 
 // Device memory of a job: stream-ordered (from the device's memory pool, on the job's stream)
 // when the job was created with stream_ordered = 1, plain otherwise.
+// Host-side fault injection for tests of the error paths: with MPSQ_FAIL_ALLOC=k in the
+// environment the k-th device allocation of every job reports cudaErrorMemoryAllocation
+// without calling the allocator.
+static bool injected_alloc_failure(mpsq_job* j) {
+  const char* e = getenv("MPSQ_FAIL_ALLOC");
+  return e && ++j->n_alloc == atoi(e);
+}
 static cudaError_t job_alloc(mpsq_job* j, void** ptr, size_t bytes) {
+  if (injected_alloc_failure(j)) {
+    *ptr = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
   bytes = std::max<size_t>(bytes, 16);
   return j->d.stream_ordered ? cudaMallocAsync(ptr, bytes, j->s) : cudaMalloc(ptr, bytes);
 }

@@ -55,3 +55,20 @@ def test_job_descriptor_bindings_match_the_header():
     # every function the Fortran module binds is exported under that name
     bound = set(re.findall(r'bind\(C, name="([a-z_0-9]+)"\)', f90))
     assert bound and bound <= set(header_functions())
+
+
+def test_injected_allocation_failure_reports_err_alloc(lib, monkeypatch):
+    """Fault injection on the host: with MPSQ_FAIL_ALLOC=1 the job's first device allocation
+    reports out-of-memory before the allocator is called, so job creation returns
+    MPSQ_ERR_ALLOC (2) with its message and no handle, on any machine."""
+    import ctypes as C
+    from mp_tools_gb300 import _lib
+    from mp_tools_gb300.sqom import QGrid, SqomJob
+    grid = QGrid(_lib.BULK, (1, 1, 1), n_bz=2.0, a_par=(10.0,) * 3, ndim=3)
+    d = SqomJob.describe(grid, species_counts=[100], n_frames=2, n_atoms_frame=100)
+    h = C.c_void_p()
+    monkeypatch.setenv("MPSQ_FAIL_ALLOC", "1")
+    assert lib.mpsq_job_create(C.byref(d), None, C.byref(h)) == 2
+    assert not h.value
+    msg = lib.mpsq_last_error()
+    assert b"job_create" in (msg if isinstance(msg, bytes) else msg.encode())
