@@ -5,10 +5,11 @@ Requests arrive over time, each an MD trajectory (host memory) with its Q grid a
 request is admitted as soon as an execution slot is free and its device footprint
 (``mpsq_job_estimate_bytes``: trajectory, fine grids, records, amplitude store) fits in what
 the admitted jobs leave of the budget; requests that could never fit are rejected, the others
-wait in arrival order.  Every admitted job runs on its own CUDA stream with stream-ordered
-device memory, so creating and closing a job never waits for the device, and the kernels of
-jobs that are in flight together overlap on the GPU (a job that arrives while others run starts
-at once instead of after them).  The host loop only launches work, polls completion events and
+wait in arrival order, and a request that is still waiting when its ``max_wait`` has passed is
+cancelled without being started (an admitted job always runs to completion).  Every admitted
+job runs on its own CUDA stream with stream-ordered device memory, so creating and closing a
+job never waits for the device, and the kernels of jobs that are in flight together overlap on
+the GPU (a job that arrives while others run starts at once instead of after them).  The host loop only launches work, polls completion events and
 admits the next requests.
 
 Per job: upload of the trajectory, the NUFFT of every frame and species with the species
@@ -16,7 +17,7 @@ weights, total S(Q) and, for runs of at least 4 frames, E=const maps of the firs
 (mp_sqom's sliding-window form), all copied back to pinned host memory; the job's latency is the
 time from its arrival to the moment its results are on the host.  ``Server.run`` returns the
 results and the stream's statistics: p50/p99 latency, throughput in nonuniform points per
-second, completed / rejected counts and the longest queue.
+second, completed / rejected / cancelled counts and the longest queue.
 """
 from __future__ import annotations
 
@@ -40,6 +41,7 @@ class Request:
     job_kwargs: dict = field(default_factory=dict)   # SqomJob arguments (precision, eps, weights)
     t_step: float = 0.01           # ps between frames (E=const maps)
     n_econst: int = 4              # E=const bins returned when the run has >= 4 frames
+    max_wait: float | None = None  # seconds it may wait for admission; cancelled after that
 
     @property
     def n_frames(self) -> int:
@@ -140,7 +142,7 @@ class Server:
         queue: deque = deque()
         active = []                # (req, handle, bytes, admitted)
         results: dict[int, Result] = {}
-        rejected, waited = [], set()
+        rejected, cancelled, waited = [], [], set()
         used = peak = 0
         max_queue = 0
         t0 = self.clock()
@@ -165,6 +167,15 @@ class Server:
                 else:
                     still.append((r, h, b, adm))
             active = still
+            # requests whose admission deadline has passed leave the queue unstarted
+            if any(r.max_wait is not None for r, _ in queue):
+                keep = deque()
+                for r, b in queue:
+                    if r.max_wait is not None and now > r.arrival + r.max_wait:
+                        cancelled.append(r.rid)
+                    else:
+                        keep.append((r, b))
+                queue = keep
             # admissions in arrival order (the head of the queue blocks the rest)
             while queue and len(active) < self.max_active and used + queue[0][1] <= self.budget:
                 r, b = queue.popleft()
@@ -184,6 +195,7 @@ class Server:
         pts = sum(r.nu_points for r in requests if r.rid in results)
         stats = {
             "completed": len(results), "rejected": len(rejected), "rejected_ids": rejected,
+            "cancelled": len(cancelled), "cancelled_ids": cancelled,
             "queued": len(waited), "max_queue": max_queue, "budget_bytes": self.budget,
             "peak_admitted_bytes": peak, "max_active": self.max_active,
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,

@@ -2,7 +2,8 @@
 
 CPU: the scheduler against a simulated executor and clock: arrival order, the memory budget
 and the slot count are never exceeded, requests too large for the budget are rejected, jobs
-that arrive while others run start as soon as memory frees, latency percentiles.
+that arrive while others run start as soon as memory frees, requests past their admission
+deadline are cancelled unstarted, latency percentiles.
 GPU: a mixed stream of ABO3 jobs of different sizes and frame counts, admitted under a budget
 that forces queueing, gives every job the same S(Q) and E=const maps as the job run alone
 (relative l2 1e-5: FP32, record order within a tile follows the binning atomics)."""
@@ -88,6 +89,25 @@ def test_scheduler_overlaps_jobs_that_fit():
                            sleep=clk.sleep).run(reqs)
     assert ex.max_concurrent == 4 and st["queued"] == 0
     assert max(r.done for r in res.values()) < 1.1      # all four ran together
+
+
+def test_scheduler_cancels_requests_past_their_admission_deadline():
+    """A request still queued when its max_wait has passed is cancelled unstarted; one admitted
+    in time runs to completion; the head of the queue leaving unblocks the requests behind."""
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    reqs = [_req(0, 0.00, 80, 2.0), _req(1, 0.01, 80, 0.5), _req(2, 0.02, 10, 0.5),
+            _req(3, 0.03, 80, 0.5)]
+    reqs[1].max_wait = 0.5            # 0 holds the memory until t = 2: 1 gives up at t = 0.51
+    reqs[2].max_wait = 5.0            # behind 1 in the queue, admitted once 1 has left
+    reqs[3].max_wait = 3.0            # admitted when 0 ends at t = 2
+    res, st = serve.Server(ex, budget_bytes=100, max_active=4, clock=clk.clock,
+                           sleep=clk.sleep).run(reqs)
+    assert st["cancelled_ids"] == [1] and st["cancelled"] == 1
+    assert sorted(res) == [0, 2, 3]
+    assert 0.5 <= res[2].admitted < 0.6      # right after 1 left the head of the queue
+    assert res[3].admitted == pytest.approx(2.0, abs=1e-3)
+    assert ex.max_used <= 100
 
 
 @pytest.mark.gpu
