@@ -301,6 +301,52 @@ def read_par(path) -> dict:
     return groups
 
 
+@dataclass
+class SqomSettings:
+    """mp_sqom's run settings from a .par file: its namelist &mp_sqom, with the values the
+    program assigns before reading it (mp_sqom56.f90:207-219; the documented defaults of the
+    .par comments for n_int, j_oneph and j_qsq, which the program leaves unset), plus
+    &mp_out's j_weight and &mp_gen's j_verb / j_proc (:153-160, :370-416)."""
+    n_int: int = 0          # time window in frames, 0 = nfile/2 (odd for S(Q,w))
+    nfile_mem: int = 200    # frames held in memory before the transform
+    nfile_step: int = 1
+    s_trig: float = 0.0     # speckle-filter trigger ratio, 0 = off
+    j_oneph: int = 0        # 1 = one-phonon mode
+    j_sq: int = 1           # 1 = S(Q,w), 0 = I(Q,t)
+    j_qsq: int = 1          # 1 keeps the Q^2 scaling, 0 divides the maps by Q^2
+    j_wind: int = 0         # spatial Hann window; forced on for non-periodic data (n_cond = 0)
+    j_interp: int = 0
+    j_test: int = 0
+    j_weight: int = 1       # 1 unit, 2 neutron b_coh, 3 X-ray form factors
+    j_verb: int = 1
+    j_proc: int = 0
+
+    def time_axis(self, nfile: int, t_step: float):
+        """The TimeAxis these settings give for nfile frames t_step apart."""
+        from .sqom import TimeAxis
+        return TimeAxis(nfile=nfile, t_step=t_step, n_int=self.n_int, j_sq=self.j_sq)
+
+
+def read_sqom_settings(path, header: dict | None = None) -> SqomSettings:
+    """Reads mp_sqom's settings from a .par file.  The reference stops when &mp_gen, &mp_out or
+    &mp_sqom is missing (mp_sqom56.f90:372-408): here that is a ValueError.  With a frame
+    header whose n_cond is 0 (non-periodic boundaries) the spatial window is switched on, as
+    the program does at :351-355."""
+    groups = read_par(path)
+    missing = [g for g in ("mp_gen", "mp_out", "mp_sqom") if not isinstance(groups.get(g), dict)]
+    if missing:
+        raise ValueError(f"{path}: namelist group(s) {', '.join(missing)} missing")
+    st = SqomSettings()
+    names = {f for f in st.__dataclass_fields__}
+    for grp, keys in (("mp_sqom", None), ("mp_out", ("j_weight",)), ("mp_gen", ("j_verb", "j_proc"))):
+        for k, v in groups[grp].items():
+            if (keys is None and k in names) or (keys is not None and k in keys):
+                setattr(st, k, type(getattr(st, k))(v))
+    if header is not None and int(header.get("n_cond", 1)) == 0:
+        st.j_wind = 1
+    return st
+
+
 def read_table(path) -> dict:
     """Reference tables (neutron_xs.txt: label b_coh[fm] ...; xray_ff.txt: label a1 b1 a2 b2 a3
     b3 a4 b4 c): {label: [values...]} of the numeric columns that follow each label."""

@@ -170,3 +170,28 @@ def test_sq_table_write_read(tmp_path):
     assert back.shape == m.shape
     # a 0.ddd mantissa keeps 3 digits: relative rounding error <= 0.0005/0.100
     assert np.allclose(back, m, rtol=5.01e-3, atol=0.0)
+
+
+def test_sqom_settings_from_par(tmp_path):
+    """&mp_sqom / &mp_out / &mp_gen of the example .par with the program's defaults for what it
+    leaves out; a missing group is an error; non-periodic data switch the spatial window on."""
+    st = io.read_sqom_settings(GOLDEN / "alu" / "Al_U_large.par")
+    assert (st.n_int, st.s_trig, st.j_oneph, st.j_qsq) == (0, 0.0, 0, 1)
+    assert (st.j_sq, st.j_wind, st.nfile_mem, st.nfile_step) == (1, 0, 200, 1)
+    assert (st.j_weight, st.j_verb, st.j_proc) == (3, 0, 0)
+    ta = st.time_axis(nfile=20, t_step=0.01)
+    assert ta.n_int == 11                      # nfile/2, made odd for S(Q,w)
+    st2 = io.read_sqom_settings(GOLDEN / "alu" / "Al_U_large.par", header={"n_cond": 0})
+    assert st2.j_wind == 1
+    text = (GOLDEN / "alu" / "Al_U_large.par").read_text()
+    i = text.index("&mp_sqom")
+    bad = tmp_path / "no_sqom.par"
+    end = text.index("\n/", i) + 2            # the group's closing slash line
+    bad.write_text(text[:i] + text[end:])
+    with pytest.raises(ValueError, match="mp_sqom"):
+        io.read_sqom_settings(bad)
+    custom = tmp_path / "custom.par"
+    custom.write_text(text.replace("n_int = 0", "n_int = 64\nj_sq = 0").replace("s_trig = 0", "s_trig = 2.5"))
+    st3 = io.read_sqom_settings(custom)
+    assert (st3.n_int, st3.j_sq, st3.s_trig) == (64, 0, 2.5)
+    assert st3.time_axis(nfile=200, t_step=0.01).n_int == 64   # I(Q,t): not made odd
