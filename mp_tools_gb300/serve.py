@@ -21,6 +21,7 @@ second, completed / rejected / cancelled counts and the longest queue.
 """
 from __future__ import annotations
 
+import json
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -122,10 +123,13 @@ class GpuExecutor:
 class Server:
     """Admission by memory and execution slots, first come first served; see the module
     docstring.  `executor` provides estimate(req) -> bytes, start(req) -> handle,
-    done(handle) -> bool and finish(handle) -> (sq, sqw)."""
+    done(handle) -> bool and finish(handle) -> (sq, sqw).  `metrics`, a writable text file,
+    receives one JSON line per completed, rejected or cancelled request and a summary line
+    with the statistics that run() returns."""
 
     def __init__(self, executor=None, budget_bytes: int | None = None, max_active: int = 8,
-                 poll_s: float = 2e-4, clock=time.perf_counter, sleep=time.sleep):
+                 poll_s: float = 2e-4, clock=time.perf_counter, sleep=time.sleep,
+                 metrics=None):
         self.ex = executor if executor is not None else GpuExecutor()
         if budget_bytes is None:
             import torch
@@ -136,6 +140,11 @@ class Server:
         self.poll_s = poll_s
         self.clock = clock
         self.sleep = sleep
+        self.metrics = metrics         # file-like: one JSON line per request event + a summary
+
+    def _emit(self, record: dict):
+        if self.metrics is not None:
+            self.metrics.write(json.dumps(record) + "\n")
 
     def run(self, requests):
         pending = deque(sorted(requests, key=lambda r: (r.arrival, r.rid)))
@@ -154,6 +163,8 @@ class Server:
                 b = self.ex.estimate(r)
                 if b > self.budget:
                     rejected.append(r.rid)
+                    self._emit({"event": "rejected", "rid": r.rid, "t_s": now, "bytes": b,
+                                "budget_bytes": self.budget})
                 else:
                     queue.append((r, b))
             # completions first: they free memory and slots
@@ -163,6 +174,10 @@ class Server:
                     sq, sqw = self.ex.finish(h)
                     t = self.clock() - t0
                     results[r.rid] = Result(r.rid, sq, sqw, r.arrival, adm, t)
+                    self._emit({"event": "completed", "rid": r.rid, "arrival_s": r.arrival,
+                                "admitted_s": adm, "done_s": t, "latency_s": t - r.arrival,
+                                "nu_points": r.nu_points, "bytes": b,
+                                "nu_pts_per_s": r.nu_points / max(t - adm, 1e-12)})
                     used -= b
                 else:
                     still.append((r, h, b, adm))
@@ -173,6 +188,8 @@ class Server:
                 for r, b in queue:
                     if r.max_wait is not None and now > r.arrival + r.max_wait:
                         cancelled.append(r.rid)
+                        self._emit({"event": "cancelled", "rid": r.rid, "t_s": now,
+                                    "waited_s": now - r.arrival})
                     else:
                         keep.append((r, b))
                 queue = keep
@@ -203,6 +220,7 @@ class Server:
             "mean_s": float(lat.mean()) if len(lat) else None,
             "wall_s": wall, "nu_pts_per_s": pts / wall if wall > 0 else None,
         }
+        self._emit(dict(stats, event="summary"))
         return results, stats
 
 

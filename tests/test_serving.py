@@ -110,6 +110,27 @@ def test_scheduler_cancels_requests_past_their_admission_deadline():
     assert ex.max_used <= 100
 
 
+def test_scheduler_metrics_json_lines():
+    """One JSON line per completed, rejected and cancelled request, then the summary."""
+    import io
+    import json
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    reqs = [_req(0, 0.0, 80, 1.0), _req(1, 0.01, 500, 0.1), _req(2, 0.02, 80, 0.1)]
+    reqs[2].max_wait = 0.2
+    sink = io.StringIO()
+    res, st = serve.Server(ex, budget_bytes=100, max_active=4, clock=clk.clock, sleep=clk.sleep,
+                           metrics=sink).run(reqs)
+    lines = [json.loads(x) for x in sink.getvalue().splitlines()]
+    ev = {(d["event"], d.get("rid")) for d in lines}
+    assert ev == {("rejected", 1), ("cancelled", 2), ("completed", 0), ("summary", None)}
+    done = next(d for d in lines if d["event"] == "completed")
+    assert done["latency_s"] == pytest.approx(res[0].latency) and done["nu_points"] == 10
+    summary = lines[-1]
+    assert summary["event"] == "summary" and summary["completed"] == 1
+    assert summary["rejected_ids"] == [1] and summary["cancelled_ids"] == [2]
+
+
 @pytest.mark.gpu
 def test_gpu_results_same_alone_and_in_the_mix(cuda):
     from mp_tools_gb300 import _lib
