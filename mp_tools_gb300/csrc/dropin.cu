@@ -171,7 +171,7 @@ extern "C" void finufft2d1_(const int64_t* nj, const double* xj, const double* y
   (void)opts;
   int rc;
   if (!nj || !iflag || !eps || !ms || !mt)
-    rc = fail(MPSQ_ERR_ARG, "finufft2d1_: null scalar argument");
+    rc = report(fail(MPSQ_ERR_ARG, "finufft2d1_: null scalar argument"));
   else {
     const int64_t m[3] = {*ms, *mt, 1};
     rc = report(run_type1<double>(2, *nj, xj, yj, nullptr, cj, *iflag, *eps, m, fk));
@@ -186,7 +186,7 @@ extern "C" void finufft3d1_(const int64_t* nj, const double* xj, const double* y
   (void)opts;
   int rc;
   if (!nj || !iflag || !eps || !ms || !mt || !mu)
-    rc = fail(MPSQ_ERR_ARG, "finufft3d1_: null scalar argument");
+    rc = report(fail(MPSQ_ERR_ARG, "finufft3d1_: null scalar argument"));
   else {
     const int64_t m[3] = {*ms, *mt, *mu};
     rc = report(run_type1<double>(3, *nj, xj, yj, zj, cj, *iflag, *eps, m, fk));

@@ -1,6 +1,7 @@
 """The C-ABI library loads and exports every entry point include/mpsq.h declares (no GPU)."""
 import re
 import subprocess
+from pathlib import Path
 
 from conftest import ROOT
 
@@ -72,3 +73,37 @@ def test_injected_allocation_failure_reports_err_alloc(lib, monkeypatch):
     assert not h.value
     msg = lib.mpsq_last_error()
     assert b"job_create" in (msg if isinstance(msg, bytes) else msg.encode())
+
+
+def test_c_caller_of_the_fortran_entry_points(lib, tmp_path):
+    """tests/abi_harness.c, compiled as C against include/mpsq.h and linked to libmpsq, calls
+    finufft2d1_ / finufft3d1_ with gfortran's by-reference convention.  On a machine with a
+    GPU the modes equal the FP64 direct sum (column-major, k1 fastest); without one every call
+    reports MPSQ_ERR_CUDA in ier, a null scalar MPSQ_ERR_ARG, and the first failure is
+    printed once to stderr (the reference never reads ier)."""
+    import numpy as np
+    import oracle
+    from mp_tools_gb300 import build as mbuild
+    so = Path(mbuild.LIB)
+    exe = tmp_path / "abi_harness"
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", str(ROOT / "include"),
+                        str(ROOT / "tests" / "abi_harness.c"), "-o", str(exe), "-L", str(so.parent),
+                        "-lmpsq", f"-Wl,-rpath,{so.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stderr
+    rows = {ln.split()[0]: ln.split()[1:] for ln in run.stdout.splitlines()}
+    ier = {k: int(v[0].split("=")[1]) for k, v in rows.items()}
+    assert ier["null"] == 1
+    x, y, z = [0.1, -1.2, 2.5], [-2.0, 0.7, 3.0], [1.5, -0.3, -3.1]
+    c = np.array([1.0, 0.5 - 0.5j, -1.0 + 2.0j])
+    if ier["2d"] == 0:
+        got = np.array([float(v) for v in rows["2d"][1:]]).view(np.complex128)
+        want = oracle.dirft2d1(x, y, c, -1, 4, 3).ravel()
+        assert np.abs(got - want).max() < 1e-7 * np.abs(want).max()
+        got3 = np.array([float(v) for v in rows["3d"][1:]]).view(np.complex128)
+        want3 = oracle.dirft3d1(x, y, z, c, -1, 4, 3, 2).ravel()
+        assert np.abs(got3 - want3).max() < 1e-7 * np.abs(want3).max()
+    else:
+        assert ier["2d"] == 3 and ier["3d"] == 3
+        assert run.stderr.count("mpsq: finufft replacement failed") == 1
