@@ -107,3 +107,23 @@ def test_c_caller_of_the_fortran_entry_points(lib, tmp_path):
     else:
         assert ier["2d"] == 3 and ier["3d"] == 3
         assert run.stderr.count("mpsq: finufft replacement failed") == 1
+
+
+def test_job_memory_estimate_structure(lib):
+    """mpsq_job_estimate_bytes (host arithmetic, used for admission): each extra frame adds its
+    16-byte positions and its row of the complex amplitude store; keeping per-species
+    amplitudes adds their store; FP64 doubles the amplitude bytes per frame."""
+    from mp_tools_gb300 import _lib
+    from mp_tools_gb300.sqom import QGrid, SqomJob
+    grid = QGrid(_lib.BULK, (1, 1, 1), n_bz=3.0, a_par=(20.0,) * 3, ndim=3)
+    nq, na = grid.n_modes, 500
+
+    def est(**kw):
+        d = SqomJob.describe(grid, species_counts=[400, 100], n_atoms_frame=na, **kw)
+        return SqomJob.estimate_bytes(d)
+
+    f1, f2 = est(n_frames=4), est(n_frames=10)
+    assert f2 - f1 == 6 * (na * 16 + nq * 8)
+    assert est(n_frames=4, store_species=True) - f1 == 4 * 2 * nq * 8
+    g1, g2 = est(n_frames=4, precision=_lib.FP64), est(n_frames=10, precision=_lib.FP64)
+    assert g2 - g1 == 6 * (na * 16 + nq * 16)
