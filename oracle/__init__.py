@@ -7,8 +7,10 @@ Contents
   * ``dirft2d1`` / ``dirft3d1`` / ``dirft_modes`` — FP64 direct type-1 sums (C, OpenMP), the
     definition the reference's own check path uses (code/src/mp_sqom56.f90:2530-2547).
   * ``es_nufft`` — a CPU port of the exponential-of-semicircle type-1 NUFFT (FP64 spreading in
-    C/OpenMP, scipy/pocketfft FFT, deconvolution by quadrature of the kernel transform), the
-    stand-in for FINUFFT+OpenMP, which is not available on either machine.
+    C/OpenMP with the points counting-sorted into 8^dim blocks and threads owning disjoint
+    planes, scipy/pocketfft FFT, deconvolution by quadrature of the kernel transform), the
+    stand-in for FINUFFT+OpenMP, which is not available on either machine; with
+    ``weight_accumulate`` / ``abs2_accumulate`` (OpenMP) it is the timed CPU baseline.
   * ``sqom_ref`` — numpy restatement of the mp_sqom loops around the NUFFT call.
   * ``sql_ref`` — numpy restatement of mp_sql's spherical average (Q cube, FP32 |Q| binning,
     normalisation, smoothing, X-ray output modes).
