@@ -42,8 +42,8 @@ def main(ref):
     ref = Path(ref)
     alu = ref / "examples" / "amorphous_Al92U08"
     (HERE / "alu").mkdir(exist_ok=True)
-    shutil.copy(alu / "data" / "Al_U_large_n0001.dat", HERE / "alu" / "Al_U_large_n0001.dat")
-    shutil.copy(alu / "Al_U_large.par", HERE / "alu" / "Al_U_large.par")
+    shutil.copyfile(alu / "data" / "Al_U_large_n0001.dat", HERE / "alu" / "Al_U_large_n0001.dat")
+    shutil.copyfile(alu / "Al_U_large.par", HERE / "alu" / "Al_U_large.par")
     arrays, metas = {}, {}
     for k, mode in ((40, 5), (41, 6), (42, 4), (43, 7)):
         meta, rows = table(alu / f"Al_U_large_sql_0001_{k}.txt")
