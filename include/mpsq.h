@@ -52,7 +52,8 @@ extern "C" {
  *   periodically).  Complex arrays are interleaved (re, im) pairs, i.e. C99 double _Complex
  *   or Fortran complex(8).  opts may be NULL (library defaults); a non-NULL opts is accepted
  *   and ignored.  The relative l2 error of fk is at most about eps (eps is clamped to
- *   [1e-14, 1e-1] for FP64 and [1e-7, 1e-1] for FP32).
+ *   [1e-14, 1e-1]) for FP64; FP32 transforms always use the kernel width of eps = 1e-6 and
+ *   reach a relative l2 error of about 2e-6 whatever eps is passed.
  */
 
 /* Replaces FINUFFT's C entry finufft2d1 — the routine mp_sqom calls once per frame and

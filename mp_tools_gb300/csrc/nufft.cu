@@ -44,6 +44,10 @@ EsKernel es_params(double eps, int precision) {
   if (eps > 1e-1) eps = 1e-1;
   int w = (int)std::ceil(std::log10(1.0 / eps)) + 1;
   w = std::max(2, std::min(16, w));
+  // FP32 transforms use the width of eps = 1e-6 whatever eps asks for: about the accuracy FP32
+  // spreading and FFTs reach (relative l2 ~2e-6), and the width at which every FP32 kernel
+  // path (tensor-core and CUDA-core spreading, 2D and 3D) is parity-tested on the GPU.
+  if (precision != MPSQ_FP64) w = 7;
   EsKernel k;
   k.w = w;
   k.beta = 2.30 * w;
