@@ -36,7 +36,7 @@ METRIC = "NU pts/s S(Q,w) FP32 batched (amorphous Al92U8, 1e6 atoms, 512 frames,
 UNIT = "NU pts/s"
 N_ATOMS, RHO, FRAC_U, DMIN = 1_000_000, 0.06, 0.08, 2.2
 FRAMES, SIGMA, T_STEP = 512, 0.1, 0.01
-Q_RANGE, EPS = 4.72, 1e-6
+Q_RANGE, EPS = 4.72, 1e-7
 SEED = 20261205
 
 
@@ -118,17 +118,18 @@ def measured_peaks():
 
 
 # ----------------------------------------------------------------------------- workload
-SPREAD_KERNEL = "spread3_pair_mma_kernel<7>"
-SPREAD_PROFILE = ROOT / "profiles" / "spread3_pair_mma_w7_alu1e6_192.txt"
+def spread_kernel_name(width):
+    return f"spread3_pair_mma_kernel<{width}>"
 
 
-def profiled_traffic():
-    """DRAM bytes (read + write) per launch of the spread kernel, from the committed summary
-    of an ncu capture of this workload (line 'traffic_bytes_per_launch: N')."""
+def profiled_traffic(width):
+    """DRAM bytes (read + write) per launch of the spread kernel at this width, from the
+    committed summary of an ncu capture of this workload (line 'traffic_bytes_per_launch: N')."""
+    path = ROOT / "profiles" / f"spread3_pair_mma_w{width}_alu1e6_192.txt"
     try:
-        for line in SPREAD_PROFILE.read_text().splitlines():
+        for line in path.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
-                return int(line.split(":")[1]), SPREAD_PROFILE.name
+                return int(line.split(":")[1]), path.name
     except OSError:
         pass
     return None, None
@@ -275,7 +276,7 @@ def accuracy_sample(job, frames_dev, counts, grid, n_q=48, n_t=3):
     nq = grid.n_modes
     qs = rng.choice(nq, n_q, replace=False)
     ts = np.linspace(0, FRAMES - 1, n_t).astype(int)
-    cs = job.amplitudes()
+    cs = job.amplitudes_at(qs, ts)
     off = np.concatenate([[0], np.cumsum(counts)])
     origin, steps, extra = grid.qphys()
     m0, m1, m2 = grid.n_q
@@ -284,17 +285,53 @@ def accuracy_sample(job, frames_dev, counts, grid, n_q=48, n_t=3):
     s2 = ((Qv ** 2).sum(1) + extra) / (16 * np.pi ** 2)
     w = [sqom_ref.xray_ff(synth.XFF[s], s2) for s in ("Al", "U")]
     got, ref = [], []
-    for t in ts:
+    for i, t in enumerate(ts):
         r_all = frames_dev[t, :, :3].double().cpu().numpy()
         acc = np.zeros(n_q, np.complex128)
         for s in range(2):
             r = r_all[off[s]:off[s + 1]]
             x = [r @ grid.axis[a].astype(np.float64) * float(grid.tpe[a]) for a in range(3)]
-            acc += w[s] * oracle.dirft_modes(x[0], x[1], x[2], np.ones(len(r)), -1, kq)
+            acc += w[s] * direct_sum(x, kq)
         ref.append(acc)
-        got.append(cs[t, qs])
+        got.append(cs[i])
     out = error_metrics(np.array(got), np.array(ref))
-    out["sample"] = f"{n_q} random Q x {n_t} frames, FP64 direct sum over all 1e6 atoms"
+    out["sample"] = (f"{n_q} random Q x {n_t} frames, FP64 direct sum over all 1e6 atoms "
+                     f"(strong samples: |F|^2 above 1e-3 of the sample maximum)")
+    return out
+
+
+def maps_accuracy(job, frames_dev, counts, grid, sq, sqw, fwhm, n_freq, n_q=40):
+    """Relative error of the job's outputs — total S(Q) and the Gaussian-window S(Q, omega) —
+    against the oracle at n_q random Q: the FP64 direct sum of every frame's weighted
+    amplitude, then the same frame sum and time transform in FP64."""
+    import torch
+
+    from oracle import sqom_ref
+    from mp_tools_gb300 import synth
+    rng = np.random.default_rng(17)
+    qs = rng.choice(grid.n_modes, n_q, replace=False)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    origin, steps, extra = grid.qphys()
+    kq = mode_index(grid, qs)
+    Qv = origin[None] + kq[:, :1] * steps[0] + kq[:, 1:2] * steps[1] + kq[:, 2:3] * steps[2]
+    s2 = ((Qv ** 2).sum(1) + extra) / (16 * np.pi ** 2)
+    w = [sqom_ref.xray_ff(synth.XFF[s], s2) for s in ("Al", "U")]
+    F = frames_dev.shape[0]
+    ref = np.zeros((F, n_q), np.complex128)
+    for t in range(F):
+        r_all = frames_dev[t, :, :3].double().cpu().numpy()
+        for s in range(2):
+            r = r_all[off[s]:off[s + 1]]
+            ref[t] += w[s] * direct_sum(grid_coords(grid, r), kq)
+    norm2 = job.norm2()
+    g = sqom_ref.gauss_window(F, fwhm)
+    qt = torch.as_tensor(qs, device="cuda")
+    out = {"sq_total": map_metrics(sq[qt].cpu().numpy(), sqom_ref.sq_total(ref, norm2)),
+           "sqw_gauss": map_metrics(sqw[:, qt].cpu().numpy(),
+                                    sqom_ref.gauss_spectrum(ref, fwhm, n_freq, None,
+                                                            T_STEP / g.sum() / norm2)),
+           "sample": f"{n_q} random Q x all {F} frames (S(Q), and {n_freq} bins each for S(Q,w)), "
+                     f"FP64 direct sum over all atoms, FP64 frame sum and time transform"}
     return out
 
 
@@ -305,10 +342,14 @@ def error_metrics(got, ref):
     ref = np.asarray(ref, np.complex128).ravel()
     s_got, s_ref = np.abs(got) ** 2, np.abs(ref) ** 2
     strong = s_ref > 1e-3 * s_ref.max()
+    rel = np.abs(s_got - s_ref) / np.maximum(s_ref, 1e-300)
+    worst = int(np.argmax(np.where(strong, rel, -1.0))) if strong.any() else None
     return {"rel_l2_amplitude": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
             "rel_l2_S": float(np.linalg.norm(s_got - s_ref) / np.linalg.norm(s_ref)),
-            "max_rel_S": (float(np.max(np.abs(s_got[strong] - s_ref[strong]) / s_ref[strong]))
-                          if strong.any() else None)}
+            "max_rel_S": float(rel[worst]) if worst is not None else None,
+            "worst_S_over_max": float(s_ref[worst] / s_ref.max()) if worst is not None else None,
+            "max_rel_S_above_1e-2_max": (float(rel[s_ref > 1e-2 * s_ref.max()].max())
+                                        if strong.any() else None)}
 
 
 def run_gpu(args):
@@ -385,7 +426,7 @@ def run_gpu(args):
     step_e2e()
     job.sync()
     barrier()
-    e_steps = max(1, min(args.steps, 3))
+    e_steps = args.steps
     e0.record(stream)
     for _ in range(e_steps):
         step_e2e()
@@ -413,15 +454,20 @@ def run_gpu(args):
     n_fine = 384 ** 3
     spread_bytes = sum(counts) * 16 + n_fine * 8
     achieved = spread_bytes / (stage["spread"] / 1e3) / 1e9
-    traffic, traffic_src = profiled_traffic()
-    roofline = {"bound": "hbm", "kernel": SPREAD_KERNEL, "achieved": achieved,
+    width = job.info()["width"]
+    traffic, traffic_src = profiled_traffic(width)
+    roofline = {"bound": "hbm", "kernel": spread_kernel_name(width), "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": spread_bytes,
                 "ms_per_launch": stage["spread"],
                 "stages_ms_per_frame": stage}
 
-    acc = accuracy_sample(job, frames, counts, grid) if rank == 0 and not args.no_accuracy else None
+    acc = None
+    if rank == 0 and not args.no_accuracy:
+        acc = {"frames": accuracy_sample(job, frames, counts, grid, n_q=args.acc_q, n_t=args.acc_t),
+               "maps": maps_accuracy(job, frames, counts, grid, sq, sqw, FRAMES / 2, n_freq,
+                                     n_q=args.acc_map_q)}
 
     # FP64 plain path on a few frames, issued per frame (one job per frame), for the ratio
     fp64 = None
@@ -548,6 +594,523 @@ def run_serving(args):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------------ further configurations
+# Seeded synthetic inputs with the shapes, sizes and distributions of the other benchmark
+# configurations (seed 20261203 + configuration index).  Each prints one JSON line of the same
+# form as the default run: device-resident value, e2e through the public API from pinned host
+# memory, the dominant kernel's roofline, the accuracy against the FP64 direct-sum oracle.
+CFG_SEED = 20261203
+ABO3_A = 4.19
+
+
+def neutron_b():
+    from mp_tools_gb300 import synth
+    return [0.1 * b for b in synth.ABO3_B_COH_FM]
+
+
+def grid_coords(grid, r):
+    """NUFFT coordinates (radians, FP64) of positions r (N x 3) on a QGrid."""
+    return [r @ grid.axis[a].astype(np.float64) * float(grid.tpe[a]) for a in range(3)]
+
+
+def oracle_amplitudes(frame, counts, grid, weights, kq):
+    """FP64 direct sum of the weighted amplitude sum_s w_s(Q) A_s(Q) of one frame (float32
+    (N, 4)) at the integer modes kq (n x 3); weights: per species, a scalar or an array over
+    the sampled modes."""
+    import oracle
+    off = np.concatenate([[0], np.cumsum(counts)])
+    r_all = np.asarray(frame[:, :3], np.float64)
+    acc = np.zeros(len(kq), np.complex128)
+    for s in range(len(counts)):
+        r = r_all[off[s]:off[s + 1]]
+        x = grid_coords(grid, r)
+        keep = ~((r[:, 0] == 0) & (r[:, 1] == 0) & (r[:, 2] == 0)) if grid.input_method == 0 else None
+        if keep is not None and not keep.all():
+            x = [c[keep] for c in x]
+        acc += np.asarray(weights[s]) * direct_sum(x, kq)
+    return acc
+
+
+def direct_sum(x, kq):
+    """FP64 direct type-1 sum of unit strengths at modes kq: per point either one exponential
+    per mode or phase tables along each axis, whichever costs less."""
+    import oracle
+    span = (kq.max(axis=0) - kq.min(axis=0) + 1).sum()
+    if 8 * len(kq) < span + 2 * len(kq):
+        return oracle.dirft_modes(x[0], x[1], x[2], np.ones(len(x[0])), -1, kq)
+    return oracle.dirft_modes_tab(x[0], x[1], x[2], np.ones(len(x[0])), -1, kq)
+
+
+def map_metrics(got, want):
+    """Relative l2 error of a map sample and the largest relative error over the samples above
+    1e-3 of the sample maximum."""
+    got = np.asarray(got, np.float64).ravel()
+    want = np.asarray(want, np.float64).ravel()
+    strong = want > 1e-3 * want.max()
+    return {"rel_l2_S": float(np.linalg.norm(got - want) / np.linalg.norm(want)),
+            "max_rel_S": float(np.max(np.abs(got[strong] - want[strong]) / want[strong]))}
+
+
+def mode_index(grid, q):
+    m0, m1, m2 = grid.n_q
+    return np.stack([q % m0 - m0 // 2, (q // m0) % m1 - m1 // 2, q // (m0 * m1) - m2 // 2], 1)
+
+
+def timed_steps(step, args, stream, L):
+    """W untimed steps, then K timed steps bracketed by synchronisation; returns ms per step,
+    the clock record and the number of this library's launches in the timed region."""
+    import torch
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+    clocks.start()
+    n0 = L.mpsq_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / args.steps, clocks.stop(), int(L.mpsq_launch_count() - n0)
+
+
+def spread_roofline(job, pts_per_frame, kernel):
+    """Stage times of one profiled transform pass; the spread kernel's algorithmic bytes
+    (16 B per point + 8 or 16 B per fine-grid cell and grid) over its CUDA-event duration."""
+    import torch
+    info = job.info()
+    job.profile(True)
+    job.stage_ms(reset=True)
+    job.transform()
+    torch.cuda.synchronize()
+    st, nfr = job.stage_ms()
+    job.profile(False)
+    stage = dict(zip(["bin", "spread", "fft", "deconv"], [v / max(nfr, 1) for v in st]))
+    nf = info["fine_grid"]
+    cell = 16 if job.precision == 1 else 8
+    ngrid = job.n_grids()
+    spread_bytes = pts_per_frame * 16 + ngrid * nf[0] * nf[1] * nf[2] * cell
+    peak, peak_kind = measured_peaks()
+    achieved = spread_bytes / (stage["spread"] / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": int(spread_bytes), "ms_per_launch": stage["spread"],
+            "stages_ms_per_frame": stage, "width": info["width"], "fine_grid": list(nf),
+            "pruned_fft": info["pruned"]}
+
+
+def cpu_port_job(frames_np, counts, grid, weights_full, eps, n_frames):
+    """The oracle's CPU port (FP64 ES NUFFT per species and frame + weighting + |F|^2) on
+    n_frames frames; returns (seconds, points, threads)."""
+    import oracle
+    off = np.concatenate([[0], np.cumsum(counts)])
+    cs = np.empty(grid.n_modes, np.complex128)
+    s_q = np.zeros(grid.n_modes, np.float64)
+    el, pts = 0.0, 0
+    for t in range(n_frames):
+        fr = frames_np[t % len(frames_np)]
+        t0 = time.perf_counter()
+        for s in range(len(counts)):
+            r = np.asarray(fr[off[s]:off[s + 1], :3], np.float64)
+            A = oracle.es_nufft(grid_coords(grid, r), np.ones(len(r)), -1, eps, grid.n_q)
+            oracle.weight_accumulate(cs, weights_full[s], A, first=(s == 0))
+        oracle.abs2_accumulate(s_q, cs)
+        el += time.perf_counter() - t0
+        pts += int(off[-1])
+    return el, pts, oracle.num_threads()
+
+
+def full_weights(grid, counts, b):
+    return [np.full(grid.n_modes, float(b[s])) for s in range(len(counts))]
+
+
+def run_config_job(name, metric, workload, args):
+    """Shared driver of the job configurations.  workload() returns a dict with: frames (torch
+    (F, N, 4) on cuda), counts, grid, job kwargs (`kw`), `maps(job, outs)` issuing the step's
+    maps into the given output tensors, `outs` (device tensors), `accuracy(job, frames)`,
+    `config` (dict), `pts_per_step`, and optional `fp64` / `cpu` callables."""
+    import torch
+
+    from mp_tools_gb300 import _lib
+    from mp_tools_gb300.sqom import SqomJob
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    L = _lib.load()
+    wl = workload()
+    stream = torch.cuda.current_stream()
+    frames, grid = wl["frames"], wl["grid"]
+    job = SqomJob(grid, species_counts=wl["counts"], n_frames=frames.shape[0],
+                  stream=stream.cuda_stream, n_atoms_frame=frames.shape[1], **wl["kw"])
+    job.set_frames(frames)
+    outs = wl["outs"]
+
+    def step():
+        job.transform()
+        wl["maps"](job, outs)
+
+    ms, clk, launches = timed_steps(step, args, stream, L)
+    value = wl["pts_per_step"] / (ms / 1e3)
+    # e2e through the public API from pinned host memory
+    host_frames, pin_f = host_buffer(frames.shape)
+    host_frames.copy_(frames)
+    host_outs = [host_buffer(o.shape) for o in outs]
+    pinned = pin_f and all(p for _, p in host_outs)
+    houts = [h for h, _ in host_outs]
+
+    def step_e2e():
+        job.transform_from_host(host_frames)
+        wl["maps"](job, houts)
+
+    step_e2e()
+    job.sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_e2e()
+    job.wait_outputs()
+    e1.record(stream)
+    job.sync()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    e2e = {"value": wl["pts_per_step"] / (ms_e2e / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": int(host_frames.numel() * 4),
+           "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in houts)), "ms_per_step": ms_e2e,
+           "host_memory": "pinned" if pinned else "pageable (pinning refused)"}
+    roof = spread_roofline(job, int(sum(wl["counts"])), wl.get("kernel", "spread"))
+    acc = None if args.no_accuracy else wl["accuracy"](job, frames, outs)
+    fp64 = wl["fp64"](stream) if (wl.get("fp64") and not args.no_fp64) else None
+    job.close()
+    cpu = wl["cpu"]() if (wl.get("cpu") and not args.no_cpu) else None
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": wl["dtype"], "data": wl["data"], "config": wl["config"],
+           "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+           "clocks": clk, "accuracy": acc, "fp64_plain": fp64}
+    print(json.dumps(out), flush=True)
+
+
+def fp64_per_frame(frames, counts, grid, kw, stream, n=2):
+    """The same frames through the FP64 plain path, one single-frame job per frame."""
+    import torch
+
+    from mp_tools_gb300 import _lib
+    from mp_tools_gb300.sqom import SqomJob
+    kw = dict(kw, precision=_lib.FP64)
+    j64 = SqomJob(grid, species_counts=counts, n_frames=1, stream=stream.cuda_stream,
+                  n_atoms_frame=frames.shape[1], no_pack=True, **kw)
+    sq = torch.empty(grid.n_modes, dtype=torch.float32, device="cuda")
+    j64.set_frames(frames[0:1])
+    j64.transform()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for t in range(n):
+        j64.set_frames(frames[t:t + 1])
+        j64.transform()
+        j64.sq_total(out=sq)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    j64.close()
+    return {"value": sum(counts) / (ms / 1e3), "unit": UNIT, "ms_per_frame": ms, "frames": n,
+            "note": "per-frame FP64 plain job (no species packing)"}
+
+
+def workload_c0():
+    """ABO3 20^3 cells (40,000 atoms), Gaussian displacements, neutron weights, one frame, 160^3
+    modes (8 zones per axis), FP64 at eps 1e-9; S(Q) checked on the central 32^3 sub-grid."""
+    import torch
+
+    from mp_tools_gb300 import _lib, synth
+    from mp_tools_gb300.sqom import QGrid
+    eps = EPS_CFG if EPS_CFG is not None else 1e-9
+    rng = np.random.default_rng(CFG_SEED + 0)
+    pos, _, counts = synth.abo3_static(20, ABO3_A, rng)
+    grid = QGrid(_lib.CELL, (20, 20, 20), n_bz=8, a_par=(ABO3_A,) * 3, ndim=3)
+    frames = torch.from_numpy(pos[None]).cuda()
+    b = neutron_b()
+    kw = dict(precision=_lib.FP64, eps=eps, weight_mode=_lib.WEIGHT_NEUTRON, b_coh=b)
+    sq = torch.empty(grid.n_modes, dtype=torch.float32, device="cuda")
+
+    def maps(job, outs):
+        job.sq_total(out=outs[0])
+
+    def accuracy(job, frames_dev, outs):
+        k = np.arange(-16, 16)
+        kz, ky, kx = np.meshgrid(k, k, k, indexing="ij")
+        kq = np.stack([kx.ravel(), ky.ravel(), kz.ravel()], 1)
+        m = np.array(grid.n_q)
+        q = ((kq[:, 2] + m[2] // 2) * m[1] + kq[:, 1] + m[1] // 2) * m[0] + kq[:, 0] + m[0] // 2
+        ref = oracle_amplitudes(pos, counts, grid, b, kq)
+        out = error_metrics(job.amplitudes_at(q)[0], ref)
+        out["sample"] = "central 32^3 sub-grid (32,768 modes), FP64 direct sum over all 40,000 atoms"
+        return out
+
+    def cpu():
+        el, pts, thr = cpu_port_job(pos[None], counts, grid, full_weights(grid, counts, b), eps, 3)
+        return {"value": pts / el, "unit": UNIT, "cores": thr, "kind": "port",
+                "sample": f"the frame 3 times, 5 species, FP64 ES NUFFT eps {eps} + weights, {el:.1f} s"}
+
+    return dict(frames=frames, counts=counts, grid=grid, kw=kw, maps=maps, outs=[sq],
+                accuracy=accuracy, cpu=cpu, pts_per_step=int(sum(counts)), dtype="f64",
+                kernel="spread_tile_kernel<double,3>",
+                data="synthetic (seeded ABO3 supercell, Gaussian displacements)",
+                config={"workload": "static S(Q) of ABO3 20^3 cells (40,000 atoms), 160^3 modes, "
+                                    "FP64 eps %g, neutron weights" % eps,
+                        "atoms": int(sum(counts)), "frames": 1, "species": 5,
+                        "modes": list(grid.n_q), "eps": eps, "precision": "fp64",
+                        "l2": "fine grid 320^3 complex128 (524 MB) larger than L2",
+                        "parallelism": "single GPU"})
+
+
+def workload_c1():
+    """ABO3 64^3 cells (1,310,720 atoms) displaced by 48 seeded plane waves, 256 frames at
+    10 fs, 256^3 modes (4 zones per axis), FP32 at eps 1e-6, neutron weights; Gaussian window
+    (FWHM 128 frames) + 256-point transform per Q, 129 bins, and two E=const maps of the
+    sliding Hann window (n_int 129, 128 start frames) at bins 5 and 17."""
+    import torch
+
+    from mp_tools_gb300 import _lib, synth
+    from mp_tools_gb300.sqom import QGrid, TimeAxis
+    from oracle import sqom_ref
+    eps = EPS_CFG if EPS_CFG is not None else 1e-6
+    F, n, dt = 256, 64, 0.01
+    rng = np.random.default_rng(CFG_SEED + 1)
+    frames, counts, _ = synth.abo3_planewave_frames(n, F, dt, ABO3_A, rng, device="cuda")
+    grid = QGrid(_lib.CELL, (n, n, n), n_bz=4, a_par=(ABO3_A,) * 3, ndim=3)
+    b = neutron_b()
+    kw = dict(precision=_lib.FP32, eps=eps, weight_mode=_lib.WEIGHT_NEUTRON, b_coh=b)
+    n_freq = F // 2 + 1
+    fwhm = F / 2
+    taxis = TimeAxis(F, dt, n_int=129)
+    bins = (5, 17)
+    outs = [torch.empty((n_freq, grid.n_modes), dtype=torch.float32, device="cuda"),
+            torch.empty(grid.n_modes, dtype=torch.float32, device="cuda")] + \
+           [torch.empty(grid.n_modes, dtype=torch.float32, device="cuda") for _ in bins]
+
+    def maps(job, o):
+        job.sqw_gauss(fwhm_frames=fwhm, n_freq=n_freq, t_step=dt, out=o[0])
+        job.sq_total(out=o[1])
+        for i, jf in enumerate(bins):
+            job.sqw_econst(taxis, jf, out=o[2 + i])
+
+    def accuracy(job, frames_dev, o):
+        # 1,000 (Q, omega) points: 40 random Q x 25 random Gaussian-spectrum bins, and the same
+        # 40 Q at the two E=const bins; the oracle forms F(Q, t) for all 256 frames by direct sum
+        # and applies the same time transforms in FP64
+        rq = np.random.default_rng(11)
+        q = rq.choice(grid.n_modes, 40, replace=False)
+        kq = mode_index(grid, q)
+        ref = np.zeros((F, len(q)), np.complex128)
+        for t in range(F):
+            ref[t] = oracle_amplitudes(frames_dev[t].cpu().numpy(), counts, grid, b, kq)
+        norm2 = job.norm2()
+        g = sqom_ref.gauss_window(F, fwhm)
+        sq_ref = sqom_ref.gauss_spectrum(ref, fwhm, n_freq, None, dt / g.sum() / norm2)
+        wbin = rq.integers(0, n_freq, (len(q), 25))
+        qt = torch.as_tensor(q, device="cuda")
+        got_g = o[0][:, qt].cpu().numpy()                    # (n_freq, 40)
+        cols = np.arange(len(q))[:, None]
+        out = {"gauss": map_metrics(got_g[wbin, cols], sq_ref[wbin, cols])}
+        tw = taxis.window().astype(np.float64)
+        for i, jf in enumerate(bins):
+            want = sqom_ref.econst(ref, taxis.n_int, tw, jf, None,
+                                   dt / (0.5 * taxis.n_frame * taxis.n_int) / norm2)
+            out[f"econst_bin{jf}"] = map_metrics(o[2 + i][qt].cpu().numpy(), want)
+        cs = job.amplitudes_at(q)
+        out["amplitudes"] = error_metrics(cs, ref)
+        out["sample"] = ("40 random Q x 25 random bins of the Gaussian spectrum (1,000 (Q,w) "
+                         "points) and the 40 Q at E=const bins 5 and 17; FP64 direct sum of all "
+                         "256 frames over all 1,310,720 atoms, FP64 time transforms")
+        return out
+
+    def fp64(stream):
+        return fp64_per_frame(frames, counts, grid, kw, stream, n=2)
+
+    def cpu():
+        fr = frames[0:1].cpu().numpy()
+        el, pts, thr = cpu_port_job(fr, counts, grid, full_weights(grid, counts, b), eps, 1)
+        return {"value": pts / el, "unit": UNIT, "cores": thr, "kind": "port",
+                "sample": f"1 frame x 5 species (1,310,720 atoms, 256^3 modes), FP64 ES NUFFT "
+                          f"eps {eps} + weights, {el:.1f} s"}
+
+    return dict(frames=frames, counts=counts, grid=grid, kw=kw, maps=maps, outs=outs,
+                accuracy=accuracy, fp64=fp64, cpu=cpu, pts_per_step=int(sum(counts)) * F,
+                dtype="f32", kernel="spread3_pair_mma_kernel",
+                data="synthetic (seeded ABO3 supercell, 48 plane-wave modes)",
+                config={"workload": "inelastic S(Q,w) of ABO3 64^3 cells (1,310,720 atoms), "
+                                    "256 frames, 256^3 modes, FP32 eps %g, neutron weights, "
+                                    "Gaussian window + sliding Hann E=const maps" % eps,
+                        "atoms": int(sum(counts)), "frames": F, "species": 5,
+                        "modes": list(grid.n_q), "eps": eps, "precision": "fp32 split",
+                        "time_transform": "Gaussian FWHM 128 frames, 256-point DFT, 129 bins; "
+                                          "sliding Hann n_int 129 at bins 5, 17; total S(Q)",
+                        "l2": "inputs larger than L2 (5.4 GB trajectory, 34 GB amplitude store)",
+                        "parallelism": "single GPU"})
+
+
+def workload_c4():
+    """ABO3 136^3 cells (12,577,280 atoms), one frame: Gaussian displacements plus 90-degree
+    domain walls (B sites +-0.1 A along z in alternating 17-cell slabs), 544^3 modes (4 zones),
+    fine grid 1152^3, FP32 spreading with FP64-exact phase reduction at eps 1e-5; 4,096 random Q
+    against the FP64 direct sum."""
+    import torch
+
+    from mp_tools_gb300 import _lib, synth
+    from mp_tools_gb300.sqom import QGrid
+    eps = EPS_CFG if EPS_CFG is not None else 1e-5
+    n = 136
+    rng = np.random.default_rng(CFG_SEED + 4)
+    shift = synth.domain_wall_shift(n, ABO3_A, rng)
+    pos, _, counts = synth.abo3_static(n, ABO3_A, rng, extra_b=shift)
+    grid = QGrid(_lib.CELL, (n, n, n), n_bz=4, a_par=(ABO3_A,) * 3, ndim=3)
+    frames = torch.from_numpy(pos[None]).cuda()
+    b = neutron_b()
+    kw = dict(precision=_lib.FP32, eps=eps, weight_mode=_lib.WEIGHT_NEUTRON, b_coh=b)
+    sq = torch.empty(grid.n_modes, dtype=torch.float32, device="cuda")
+
+    def maps(job, outs):
+        job.sq_total(out=outs[0])
+
+    def accuracy(job, frames_dev, outs):
+        rq = np.random.default_rng(13)
+        q = rq.choice(grid.n_modes, 4096, replace=False)
+        ref = oracle_amplitudes(pos, counts, grid, b, mode_index(grid, q))
+        out = error_metrics(job.amplitudes_at(q)[0], ref)
+        out["sample"] = "4,096 random Q, FP64 direct sum over all 12,577,280 atoms"
+        return out
+
+    def cpu():
+        import oracle
+        off = np.concatenate([[0], np.cumsum(counts)])
+        r = np.asarray(pos[off[1]:off[2], :3], np.float64)
+        t0 = time.perf_counter()
+        oracle.es_nufft(grid_coords(grid, r), np.ones(len(r)), -1, eps, grid.n_q)
+        el = time.perf_counter() - t0
+        return {"value": len(r) / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                "sample": f"one species transform (B sites, 2,515,456 atoms, 544^3 modes, fine "
+                          f"grid 1152^3 complex128), FP64 ES NUFFT eps {eps}, {el:.1f} s"}
+
+    return dict(frames=frames, counts=counts, grid=grid, kw=kw, maps=maps, outs=[sq],
+                accuracy=accuracy, cpu=cpu, pts_per_step=int(sum(counts)), dtype="f32",
+                kernel="spread3_pair_mma_kernel",
+                data="synthetic (seeded ABO3 supercell, Gaussian displacements, domain walls)",
+                config={"workload": "large static S(Q) of ABO3 136^3 cells (12,577,280 atoms), "
+                                    "544^3 modes, fine grid 1152^3, FP32 eps %g" % eps,
+                        "atoms": int(sum(counts)), "frames": 1, "species": 5,
+                        "modes": list(grid.n_q), "eps": eps, "precision": "fp32 split",
+                        "l2": "fine grids of 12.2 GB each, larger than L2",
+                        "parallelism": "single GPU"})
+
+
+def run_dropin2d(args):
+    """The reference's own call pattern through the drop-in boundary: an unmodified mp_sqom
+    calls finufft2d1_ (Fortran convention, every argument by reference, host arrays, NULL
+    opts) once per frame and species on the (hk0) plane (code/src/mp_sqom56.f90:1144-1156).
+    Workload of the reference's BZO example log (examples/single_crystal_BZO/
+    mp_sqom_cmd_log.txt): ABO3 32^3 cells (163,840 atoms, 5 species of 32,768), 160 x 160
+    modes (5 zones, Q centre (2 2 0)), 20 frames x 5 species = 100 calls at eps 1e-6.  value: NU points per
+    second of the calls, host arrays in and out (the e2e form is the only form this boundary
+    has); the CPU port times the same calls."""
+    import ctypes as C
+
+    import torch
+
+    import oracle
+    from mp_tools_gb300 import _lib, synth
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    L = _lib.load()
+    eps = EPS_CFG if EPS_CFG is not None else 1e-6
+    n, F, ms = 32, 20, 160
+    rng = np.random.default_rng(CFG_SEED + 5)
+    calls = []                     # (xf, yf, cf) per frame and species, as mp_sqom prepares them
+    for t in range(F):
+        pos, _, counts = synth.abo3_static(n, ABO3_A, rng)
+        off = np.concatenate([[0], np.cumsum(counts)])
+        for sp in range(5):
+            r = pos[off[sp]:off[sp + 1], :3].astype(np.float32)
+            tpe = np.float32(2 * np.pi / n)
+            xf = np.ascontiguousarray((r[:, 0] * tpe).astype(np.float64))
+            yf = np.ascontiguousarray((r[:, 1] * tpe).astype(np.float64))
+            # Q centre (2 2 0) of the example: strengths exp(-2 pi i q_c . r) (:1101-1117)
+            cf = np.exp(-2j * np.pi * (2.0 * r[:, 0].astype(np.float64) + 2.0 * r[:, 1]))
+            calls.append((xf, yf, np.ascontiguousarray(cf)))
+    fk = np.zeros(ms * ms, np.complex128)
+    dp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    m1, m2, iflag, epsc, ier = C.c_int64(ms), C.c_int64(ms), C.c_int(-1), C.c_double(eps), C.c_int(0)
+
+    def one(xf, yf, cf):
+        nj = C.c_int64(len(xf))
+        L.finufft2d1_(C.byref(nj), dp(xf), dp(yf), dp(cf), C.byref(iflag), C.byref(epsc),
+                      C.byref(m1), C.byref(m2), dp(fk), None, C.byref(ier))
+        if ier.value != 0:
+            raise RuntimeError(L.mpsq_last_error())
+
+    def step():
+        for c in calls:
+            one(*c)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+    clocks.start()
+    n0 = L.mpsq_launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = (time.perf_counter() - t0) / args.steps
+    launches = int(L.mpsq_launch_count() - n0)
+    clk = clocks.stop()
+    pts = sum(len(c[0]) for c in calls)
+    # accuracy of one call against the FP64 direct sum (all 160 x 160 modes)
+    xf, yf, cf = calls[1]
+    one(xf, yf, cf)
+    ref = oracle.dirft2d1(xf, yf, cf, -1, ms, ms).ravel()
+    acc = error_metrics(fk.copy(), ref)
+    acc["sample"] = "one call (B sites of frame 1, 32,768 points), all 160 x 160 modes, FP64 direct sum"
+    cpu = None
+    if not args.no_cpu:
+        oracle.es_nufft([calls[0][0], calls[0][1]], calls[0][2], -1, eps, (ms, ms))
+        t0 = time.perf_counter()
+        for c in calls:
+            oracle.es_nufft([c[0], c[1]], c[2], -1, eps, (ms, ms))
+        el_cpu = time.perf_counter() - t0
+        cpu = {"value": pts / el_cpu, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"the same 100 calls (20 frames x 5 species, 32,768 points, 160 x 160 "
+                         f"modes), FP64 ES NUFFT eps {eps}, {el_cpu:.2f} s"}
+    out = {"metric": "NU pts/s finufft2d1_ drop-in calls (BZO 32^3 cells, 100 x 32,768 pts, 160^2 Q)",
+           "value": pts / el, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * el, "ms_per_call": 1e3 * el / len(calls),
+           "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ABO3 32^3 supercells)",
+           "config": {"workload": "mp_sqom's call pattern through finufft2d1_: 20 frames x 5 "
+                                  "species, 32,768 points per call, 160 x 160 modes, eps %g, "
+                                  "host arrays by reference" % eps,
+                      "calls_per_step": len(calls), "points_per_call": 32768, "modes": [ms, ms],
+                      "eps": eps, "precision": "fp64", "parallelism": "single GPU"},
+           "reference_published": {"value": 100 * 32768 / 0.825, "unit": UNIT,
+                                   "note": "the reference's own log: 0.825 s for 100 transforms "
+                                           "of 32,768 points onto 160^2 (FINUFFT + OpenMP, its "
+                                           "machine)"},
+           "e2e": {"value": pts / el, "unit": UNIT,
+                   "h2d_bytes_per_step": int(sum(32 * len(c[0]) for c in calls)),
+                   "d2h_bytes_per_step": int(len(calls) * fk.nbytes), "ms_per_step": 1e3 * el},
+           "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk, "accuracy": acc}
+    print(json.dumps(out), flush=True)
+
+
+EPS_CFG = None
+CONFIGS = {
+    "c0": ("NU pts/s static S(Q) FP64 plain (ABO3 20^3 cells, 40,000 atoms, 160^3 Q, eps 1e-9)",
+           workload_c0),
+    "c1": ("NU pts/s S(Q,w) FP32 batched (ABO3 64^3 cells, 1.31e6 atoms, 256 frames, 256^3 Q)",
+           workload_c1),
+    "c4": ("NU pts/s static S(Q) FP32 (ABO3 136^3 cells, 1.26e7 atoms, 544^3 Q)", workload_c4),
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-case", action="store_true",
@@ -561,6 +1124,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--acc-q", type=int, default=1000, help="random Q modes of the accuracy sample")
+    ap.add_argument("--acc-t", type=int, default=3, help="frames of the accuracy sample")
+    ap.add_argument("--acc-map-q", type=int, default=40,
+                    help="random Q of the S(Q) / S(Q,w) accuracy sample (all frames)")
+    ap.add_argument("--eps", type=float, default=None, help="NUFFT tolerance (default: the config's)")
+    ap.add_argument("--config", default="c2", choices=["c0", "c1", "c2", "c4", "dropin2d"],
+                    help="workload: c2 the batched amorphous alloy (default, the headline); c0 "
+                         "static FP64 ABO3 20^3; c1 inelastic ABO3 64^3 x 256 frames; c4 static "
+                         "ABO3 136^3; dropin2d mp_sqom's own finufft2d1_ call pattern")
     ap.add_argument("--serving", action="store_true",
                     help="run the serving stream (request server) instead of the batched job")
     ap.add_argument("--serving-jobs", type=int, default=40)
@@ -573,6 +1145,17 @@ def main():
     ap.add_argument("--serving-slots", type=int, default=8)
     ap.add_argument("--serving-fp64-jobs", type=int, default=6)
     args = ap.parse_args()
+    if args.eps is not None:
+        global EPS, EPS_CFG
+        EPS = args.eps
+        EPS_CFG = args.eps
+    if args.config == "dropin2d" and args.impl != "reference":
+        run_dropin2d(args)
+        return
+    if args.config != "c2" and args.impl != "reference" and not args.serving:
+        metric, wl = CONFIGS[args.config]
+        run_config_job(args.config, metric, wl, args)
+        return
     if args.serving:
         run_serving(args)
     elif args.profile_case:

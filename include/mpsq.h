@@ -52,8 +52,8 @@ extern "C" {
  *   periodically).  Complex arrays are interleaved (re, im) pairs, i.e. C99 double _Complex
  *   or Fortran complex(8).  opts may be NULL (library defaults); a non-NULL opts is accepted
  *   and ignored.  The relative l2 error of fk is at most about eps (eps is clamped to
- *   [1e-14, 1e-1]) for FP64; FP32 transforms always use the kernel width of eps = 1e-6 and
- *   reach a relative l2 error of about 2e-6 whatever eps is passed.
+ *   [1e-14, 1e-1]) for FP64; FP32 transforms clamp eps to [1e-7, 1e-1] (kernel widths 2..8;
+ *   at 1e-7 the relative l2 error is a few 1e-7, set by FP32 rounding).
  */
 
 /* Replaces FINUFFT's C entry finufft2d1 — the routine mp_sqom calls once per frame and
@@ -285,6 +285,40 @@ int mpsq_job_transform_onephonon(mpsq_job* job, int32_t first, int32_t count, in
 /* Synchronise the job's stream. */
 int mpsq_job_sync(mpsq_job* job);
 
+/* Run-time choices of a job (no reference counterpart; FINUFFT's opts play this role).  Any
+ * change drops the job's captured graphs.
+ *   MPSQ_OPT_GRAPH  0 (default): every transform call issues its kernels on the job's stream;
+ *                   1: the frame loop of a call is captured once per (first, count) as a CUDA
+ *                   graph and replayed with one graph launch.
+ *   MPSQ_OPT_SPREAD 0 (default): tensor-core spreading of packed real species pairs;
+ *                   1: the CUDA-core FP32 spreading kernel.
+ *   MPSQ_OPT_XROWS  rows per CTA of the pruned X pass, 4 or 8 (default).
+ *   MPSQ_OPT_LANES  frame lanes used when the job has a second one, 1 or 2 (default). */
+#define MPSQ_OPT_GRAPH   1
+#define MPSQ_OPT_SPREAD  2
+#define MPSQ_OPT_XROWS   3
+#define MPSQ_OPT_LANES   4
+int mpsq_job_set_option(mpsq_job* job, int option, int value);
+int mpsq_job_get_option(const mpsq_job* job, int option, int* value);
+
+/* Autotuner (no reference counterpart): times mpsq_job_transform(job, first, count) under
+ * every combination of the choices above that applies to the job (graph replay, spreading
+ * kernel, X-pass rows, frame lanes; three calls each, the first untimed), keeps the fastest
+ * and sets it on the job.  With a cache_path, a choice recorded there for the same job shape
+ * (precision, fine grid, width, grids, packing, pruned transform, lanes) and SM count is taken
+ * without timing, and a new choice is appended.  choice[4] (optional) returns
+ * {graph, spread, xrows, lanes}; best_ms (optional) the time of one call.  The timed calls
+ * rewrite the amplitudes of the same frames. */
+int mpsq_job_autotune(mpsq_job* job, int32_t first, int32_t count, const char* cache_path,
+                      int* choice, double* best_ms);
+
+/* How a job runs (for reports and tests; no reference counterpart, FINUFFT's plan fields):
+ * spreading width, fine-grid lengths [3], number of fine grids per frame (species pairs share
+ * one), 1 when the fine-grid transform takes the pruned three-pass kernels (0: cuFFT + separate
+ * deconvolution), number of frame lanes (1 or 2).  Any output pointer may be NULL. */
+int mpsq_job_info(const mpsq_job* job, int* width, int64_t* fine_grid, int* n_grids, int* pruned,
+                  int* lanes);
+
 /* Stage timing with CUDA events on the job's stream.  enable != 0 makes mpsq_job_transform
  * record events around each stage of every frame (and wait for each frame); the accumulated
  * milliseconds of [bin, spread, fft, deconv] and the number of frames timed are returned by
@@ -294,15 +328,19 @@ int mpsq_job_stage_ms(mpsq_job* job, double* ms4, int64_t* frames, int reset);
 
 /* ---- allocation-free 2D type-1 transform -------------------------------------------
  * No counterpart in the reference: an extra entry point of this library for callers that
- * cannot allocate device memory during the call — code running while a CUDA graph is being
- * captured, hosts whose device memory is owned by their own pool, plug-in hosts that forbid
- * allocation.  Same transform and mode order as finufft2d1 (FP64), but every array is a
- * DEVICE pointer and all scratch (fine grid, bins, point records) lives in a 16 MiB static
- * device array that each GPU loading the library keeps until process exit.  Limits:
- * nj <= 65536 points, ms, mt <= 256 modes; larger sizes return MPSQ_ERR_ARG.  Synchronous on
- * `stream` (a cudaStream_t, NULL = default).  The first call on a device looks up the static
- * array's address (once per device), so make it before any stream capture.  Calls that
- * overlap on the GPU share the array and race: serialise them. */
+ * cannot allocate device memory during the call — hosts whose device memory is owned by their
+ * own pool under a fixed budget, plug-in hosts that forbid allocation inside a call.  Same
+ * transform and mode order as finufft2d1 (FP64), but every array is a DEVICE pointer and all
+ * scratch (fine grid, bins, point records, deconvolution factors) lives in a 16 MiB static
+ * device array that each GPU loading the library keeps until process exit; it calls no
+ * allocator and copies nothing from host memory.  Limits: nj <= 65536 points, ms, mt <= 256
+ * modes; larger sizes return MPSQ_ERR_ARG before anything is launched.  Synchronous on
+ * `stream` (a cudaStream_t, NULL = default): it returns after reading the device error flag.
+ * The first call on a device looks up the static array's address (once per device, with that
+ * device current), so make that first call before any stream capture.  Every call reuses the
+ * same array, which keeps the previous call's contents (the call clears what must start at
+ * zero); calls that overlap on the GPU (other host threads, other streams) race on it and
+ * must be serialised by the caller. */
 int mpsq_nufft2d1_noalloc(int64_t nj, const double* x, const double* y, const double* c,
                           int iflag, double eps, int64_t ms, int64_t mt, double* fk,
                           void* stream);

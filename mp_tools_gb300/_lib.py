@@ -15,6 +15,7 @@ FP32, FP64 = 0, 1
 CELL, BULK = 0, 1
 WEIGHT_UNIT, WEIGHT_NEUTRON, WEIGHT_XRAY = 1, 2, 3
 FF_MP_SQOM, FF_STANDARD = 0, 1
+OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES = 1, 2, 3, 4
 
 ERR_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_ALLOC", 3: "ERR_CUDA", 4: "ERR_CUFFT",
              5: "ERR_STATE", 6: "ERR_DEVICE"}
@@ -29,7 +30,8 @@ EXPORTS = [
     "mpsq_job_set_cell_index", "mpsq_job_transform", "mpsq_job_amplitudes", "mpsq_job_sq_total",
     "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_econst_pair",
     "mpsq_job_sqw_dispersion_pair", "mpsq_job_iqt", "mpsq_job_iqt_dispersion",
-    "mpsq_job_sqw_gauss", "mpsq_job_sync",
+    "mpsq_job_sqw_gauss", "mpsq_job_sync", "mpsq_job_info", "mpsq_job_set_option",
+    "mpsq_job_get_option", "mpsq_job_autotune",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
     "mpsq_version", "mpsq_launch_count",
     "mpsq_nufft2d1_noalloc", "mpsq_speckle_filter", "mpsq_job_transform_onephonon",
@@ -124,6 +126,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_job_iqt": (C.c_int, [vp, i32, i32, vp, dbl, vp, C.c_int]),
         "mpsq_job_iqt_dispersion": (C.c_int, [vp, i32, i32, vp, vp, dbl, vp, C.c_int]),
         "mpsq_job_sync": (C.c_int, [vp]),
+        "mpsq_job_info": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+        "mpsq_job_set_option": (C.c_int, [vp, C.c_int, C.c_int]),
+        "mpsq_job_get_option": (C.c_int, [vp, C.c_int, vp]),
+        "mpsq_job_autotune": (C.c_int, [vp, i32, i32, C.c_char_p, vp, vp]),
         "mpsq_job_profile": (C.c_int, [vp, C.c_int]),
         "mpsq_job_stage_ms": (C.c_int, [vp, vp, vp, C.c_int]),
         "mpsq_job_radial_hist": (C.c_int, [vp, vp, vp, dbl, dbl, i32, dbl, vp, C.c_int]),

@@ -378,11 +378,10 @@ __device__ __forceinline__ void dif_twiddles(float2* tw) {
 }
 
 // Fine-grid lengths with compiled pruned passes: the two-stage plans (64 = 8*8, 96 = 16*6,
-// 128 = 16*8, 192 = 16*12, 256 = 16*16, 384 = 16*24) and 1024 (8*8*8*2), each exercised on
-// the GPU by a parity test (against the direct sum, the cuFFT path or the reference's own
-// tables).  Other 2,3,5-smooth lengths, whose plans have radix-3, -4 or -5 stages, take the
-// cuFFT path until a parity test covers them.
-#define MPSQ_FFT_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(1024)
+// 128 = 16*8, 192 = 16*12, 256 = 16*16, 384 = 16*24) and the greedy plans 512 (8*8*8), 1024
+// (8*8*8*2) and 1152 (8*8*6*3), each exercised on the GPU by a parity test against the FP64
+// direct sum.  Other 2,3,5-smooth lengths take the cuFFT path until a parity test covers them.
+#define MPSQ_FFT_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024) X(1152)
 
 inline bool fft_size_compiled(int n) {
   switch (n) {

@@ -9,9 +9,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "fft_smem.cuh"
@@ -158,6 +160,17 @@ struct mpsq_job {
   cufftHandle oneph_fft = 0;
   bool have_oneph_fft = false;
   int n_alloc = 0;  // device allocations made so far (fault injection below)
+  // run-time choices (mpsq_job_set_option / mpsq_job_autotune)
+  int opt_graph = 0;        // replay the frame loop of a transform call as a captured graph
+  int opt_spread = 0;       // 0: tensor-core spreading of real pairs, 1: CUDA-core kernel
+  int opt_xrows = 8;        // rows per CTA of the pruned X pass (4 or 8)
+  int opt_lanes = 2;        // frame lanes used when a second lane exists (1 or 2)
+  struct Graph {
+    int32_t first, count;
+    cudaGraphExec_t exec;
+    int64_t launches;
+  };
+  std::vector<Graph> graphs;  // captured frame loops, by (first, count)
 };
 
 // Device memory of a job: stream-ordered (from the device's memory pool, on the job's stream)
@@ -962,6 +975,7 @@ struct PruneLaunch {
   float2* b2;
   int n[3], m[3], h[3], K[3];
   int ngrid, ngroups;
+  int xrows = kPassLinesX;   // rows per CTA of the X pass (4 or 8)
   const float2* tw[3];
   const float* c[3];
   cudaStream_t s;
@@ -972,16 +986,19 @@ static size_t pass_smem(int lines) {
   return (size_t)N * lines * sizeof(float2) + (size_t)N * sizeof(float2);
 }
 
-template <int N>
-static int launch_prune_x(const PruneLaunch& p) {
+template <int N, int L>
+static int launch_prune_x_l(const PruneLaunch& p) {
   const int n_rows = p.n[1] * p.n[2];
-  constexpr int L = kPassLinesX;
   const size_t sm = pass_smem<N>(L);
   cudaFuncSetAttribute(fftx_dif_kernel<N, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   fftx_dif_kernel<N, L><<<dim3((unsigned)((n_rows + L - 1) / L), (unsigned)p.ngrid), 16 * L, sm,
                           p.s>>>(p.fine, p.n_fine, n_rows, p.tw[0], p.h[0], p.K[0], p.b1);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
+}
+template <int N>
+static int launch_prune_x(const PruneLaunch& p) {
+  return p.xrows == 4 ? launch_prune_x_l<N, 4>(p) : launch_prune_x_l<N, kPassLinesX>(p);
 }
 template <int N>
 static int launch_prune_y(const PruneLaunch& p) {
@@ -1113,6 +1130,7 @@ static void job_free(mpsq_job* j) {
   if (j->have_oneph_fft) cufftDestroy(j->oneph_fft);
   job_release(j, j->oneph_u);
   job_release(j, j->oneph_base);
+  for (auto& gr : j->graphs) cudaGraphExecDestroy(gr.exec);
   if (j->fork) cudaEventDestroy(j->fork);
   if (j->join) cudaEventDestroy(j->join);
   if (j->s2) cudaStreamDestroy(j->s2);
@@ -1352,13 +1370,14 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
                   "job_create (pruned transform): %s", cudaGetErrorString(e));
     }
     j->pruned = true;
-    // second lane when its scratch is small next to the free device memory
+    // second lane (frames alternate between two streams) for multi-frame jobs when its scratch
+    // is small next to the free device memory
     const char* lanes = getenv("MPSQ_LANES");
     const size_t extra = (size_t)a.ngrid * j->g.n_fine * cs + 2 * sizeof(int) * (nkeys + 1) +
                          (size_t)j->cap * (rsize(prec) + cs) +
                          sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0];
     size_t free_b = 0, total_b = 0;
-    if (!d->stream_ordered && !(lanes && strcmp(lanes, "1") == 0) &&
+    if (!d->stream_ordered && d->n_frames > 1 && !(lanes && strcmp(lanes, "1") == 0) &&
         cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && extra * 4 < free_b) {
       cudaError_t e2 = cudaStreamCreateWithFlags(&j->s2, cudaStreamNonBlocking);
       if (e2 == cudaSuccess) e2 = cudaEventCreateWithFlags(&j->fork, cudaEventDisableTiming);
@@ -1436,7 +1455,7 @@ extern "C" int mpsq_job_set_cell_index(mpsq_job* j, const int32_t* at_ind, int h
 }
 
 template <typename T>
-static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
+static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
   using C = typename Cplx<T>::type;
   using R = typename RecOf<T>::type;
   cudaStream_t s = j->s;  // the stream of the current frame's lane
@@ -1453,7 +1472,7 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
   // two lanes: even frames of the call on the job's stream, odd ones on the second lane,
   // which first waits for everything queued on the job's stream (uploads included); the
   // job's stream waits for the second lane at the end
-  const bool two = j->lane2 && !prof && count > 1;
+  const bool two = j->lane2 && j->opt_lanes == 2 && !prof && count > 1;
   cudaStream_t const main_s = j->s;
   // locality order from the first frame (atoms move little between frames; any order gives the
   // same records, a spatial one lets a warp's cursor atomics combine)
@@ -1504,7 +1523,8 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
       MPSQ_LAUNCH_CHECK();
     }
     if (mark(1)) return MPSQ_ERR_CUDA;
-    rc = launch_spread<T>(a, (const R*)recs, (const C*)str, starts, j->pa.pack != 0, (C*)fine, s);
+    rc = launch_spread<T>(a, (const R*)recs, (const C*)str, starts, j->pa.pack != 0, (C*)fine, s,
+                          j->opt_spread == 0);
     if (rc) return rc;
     if (mark(2)) return MPSQ_ERR_CUDA;
     C* csf = (C*)j->cs + (size_t)t * nm;
@@ -1527,6 +1547,7 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
         }
         pl.ngrid = a.ngrid;
         pl.ngroups = j->ngroups;
+        pl.xrows = j->opt_xrows;
         pl.s = s;
         rc = run_pruned(pl, j->wa, (float2*)csf, (float2*)css, prof ? j->ev[3] : nullptr);
         if (rc) return rc;
@@ -1561,12 +1582,211 @@ static int job_transform_t(mpsq_job* j, int32_t first, int32_t count) {
   return MPSQ_OK;
 }
 
+static int job_transform_direct(mpsq_job* j, int32_t first, int32_t count) {
+  return j->d.precision == MPSQ_FP64 ? job_transform_body<double>(j, first, count)
+                                     : job_transform_body<float>(j, first, count);
+}
+
+// The frame loop of one transform call captured once as a CUDA graph (per (first, count)) and
+// replayed: the same kernels and copies, issued by one graph launch instead of ~7 launches per
+// frame.  Capture runs on a private stream (the job's stream may be the legacy default stream,
+// which cannot be captured); the graph is launched on the job's stream.
+static int job_transform_graph(mpsq_job* j, int32_t first, int32_t count) {
+  for (const auto& gr : j->graphs) {
+    if (gr.first == first && gr.count == count) {
+      MPSQ_CUDA_TRY(cudaGraphLaunch(gr.exec, j->s));
+      count_launch((int)gr.launches);
+      return MPSQ_OK;
+    }
+  }
+  cudaStream_t cap = nullptr;
+  MPSQ_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaStream_t const user = j->s;
+  const int64_t n0 = g_launches.load();
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  int rc = MPSQ_OK;
+  if (e == cudaSuccess) {
+    j->s = cap;
+    rc = job_transform_direct(j, first, count);
+    j->s = user;
+  }
+  cudaGraph_t graph = nullptr;
+  if (e == cudaSuccess) {
+    const cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
+    if (rc == MPSQ_OK) e = e2;
+  }
+  const int64_t launches = g_launches.load() - n0;
+  count_launch(-(int)launches);      // captured, not run
+  cudaGraphExec_t exec = nullptr;
+  if (e == cudaSuccess && rc == MPSQ_OK) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(cap);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(MPSQ_ERR_CUDA, "transform graph: %s", cudaGetErrorString(e));
+  if (j->graphs.size() >= 16) {      // bounded cache: drop the oldest
+    cudaGraphExecDestroy(j->graphs.front().exec);
+    j->graphs.erase(j->graphs.begin());
+  }
+  j->graphs.push_back({first, count, exec, launches});
+  MPSQ_CUDA_TRY(cudaGraphLaunch(exec, j->s));
+  count_launch((int)launches);
+  return MPSQ_OK;
+}
+
 extern "C" int mpsq_job_transform(mpsq_job* j, int32_t first, int32_t count) {
   if (!j) return fail(MPSQ_ERR_ARG, "transform: null job");
   if (first < 0 || count < 0 || first + count > j->d.n_frames)
     return fail(MPSQ_ERR_ARG, "transform: frames outside the trajectory");
-  return j->d.precision == MPSQ_FP64 ? job_transform_t<double>(j, first, count)
-                                     : job_transform_t<float>(j, first, count);
+  if (j->opt_graph && !j->profile && count > 0) return job_transform_graph(j, first, count);
+  return job_transform_direct(j, first, count);
+}
+
+static void drop_graphs(mpsq_job* j) {
+  for (auto& gr : j->graphs) cudaGraphExecDestroy(gr.exec);
+  j->graphs.clear();
+}
+
+extern "C" int mpsq_job_set_option(mpsq_job* j, int option, int value) {
+  if (!j) return fail(MPSQ_ERR_ARG, "set_option: null job");
+  switch (option) {
+    case MPSQ_OPT_GRAPH:
+      if (value != 0 && value != 1) return fail(MPSQ_ERR_ARG, "set_option: graph must be 0 or 1");
+      j->opt_graph = value;
+      break;
+    case MPSQ_OPT_SPREAD:
+      if (value != 0 && value != 1) return fail(MPSQ_ERR_ARG, "set_option: spread must be 0 or 1");
+      j->opt_spread = value;
+      break;
+    case MPSQ_OPT_XROWS:
+      if (value != 4 && value != 8) return fail(MPSQ_ERR_ARG, "set_option: X rows must be 4 or 8");
+      j->opt_xrows = value;
+      break;
+    case MPSQ_OPT_LANES:
+      if (value != 1 && value != 2) return fail(MPSQ_ERR_ARG, "set_option: lanes must be 1 or 2");
+      j->opt_lanes = value;
+      break;
+    default:
+      return fail(MPSQ_ERR_ARG, "set_option: unknown option %d", option);
+  }
+  drop_graphs(j);   // captured graphs hold the previous choice
+  return MPSQ_OK;
+}
+
+// Autotuner: times the transform of frames [first, first + count) under every combination of
+// the run-time choices that applies to this job (spreading kernel, X-pass rows, frame lanes,
+// graph replay), keeps the fastest and, given a cache file, records it there under a key of the
+// job's shape and the device's SM count, so that later jobs of the same shape take the choice
+// without timing.  Cache lines: "<key> <graph> <spread> <xrows> <lanes> <ms>".
+static std::string tune_key(const mpsq_job* j) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  char buf[256];
+  snprintf(buf, sizeof(buf), "mpsq-tune-1:p%d:d%d:n%lldx%lldx%lld:w%d:g%d:pk%d:pr%d:l%d:sm%d",
+           j->d.precision, j->d.ndim, (long long)j->g.nf[0], (long long)j->g.nf[1],
+           (long long)j->g.nf[2], j->es.w, j->sa.ngrid, j->pa.pack, j->pruned ? 1 : 0,
+           j->lane2 ? 1 : 0, sms);
+  return buf;
+}
+
+extern "C" int mpsq_job_autotune(mpsq_job* j, int32_t first, int32_t count, const char* cache_path,
+                                 int* choice, double* best_ms) {
+  if (!j) return fail(MPSQ_ERR_ARG, "autotune: null job");
+  if (first < 0 || count < 1 || first + count > j->d.n_frames)
+    return fail(MPSQ_ERR_ARG, "autotune: frames outside the trajectory");
+  const std::string key = tune_key(j);
+  int best[4] = {j->opt_graph, j->opt_spread, j->opt_xrows, j->opt_lanes};
+  double best_t = -1.0;
+  if (cache_path && *cache_path) {
+    if (FILE* f = fopen(cache_path, "r")) {
+      char k[256];
+      int g, sp, xr, ln;
+      double ms;
+      while (fscanf(f, "%255s %d %d %d %d %lf", k, &g, &sp, &xr, &ln, &ms) == 6) {
+        if (key == k) {
+          best[0] = g;
+          best[1] = sp;
+          best[2] = xr;
+          best[3] = ln;
+          best_t = ms;
+        }
+      }
+      fclose(f);
+    }
+  }
+  const bool cached = best_t >= 0.0;
+  if (!cached) {
+    const bool fma_ok = j->d.precision == MPSQ_FP32 && j->d.ndim == 3 && j->pa.pack != 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    MPSQ_CUDA_TRY(cudaEventCreate(&e0));
+    MPSQ_CUDA_TRY(cudaEventCreate(&e1));
+    int rc = MPSQ_OK;
+    for (int g = 0; g <= 1 && !rc; ++g)
+      for (int sp = 0; sp <= (fma_ok ? 1 : 0) && !rc; ++sp)
+        for (int xr : {8, 4}) {
+          if (rc || (!j->pruned && xr == 4)) continue;
+          for (int ln = 2; ln >= 1 && !rc; --ln) {
+            if (!j->lane2 && ln == 2) continue;
+            j->opt_graph = g;
+            j->opt_spread = sp;
+            j->opt_xrows = xr;
+            j->opt_lanes = ln;
+            drop_graphs(j);
+            rc = mpsq_job_transform(j, first, count);           // warm-up (and capture)
+            if (!rc && cudaEventRecord(e0, j->s) != cudaSuccess) rc = MPSQ_ERR_CUDA;
+            for (int r = 0; r < 2 && !rc; ++r) rc = mpsq_job_transform(j, first, count);
+            if (!rc && cudaEventRecord(e1, j->s) != cudaSuccess) rc = MPSQ_ERR_CUDA;
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = MPSQ_ERR_CUDA;
+            float ms = 0.0f;
+            if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = MPSQ_ERR_CUDA;
+            ms *= 0.5f;
+            if (!rc && (best_t < 0.0 || ms < best_t)) {
+              best_t = ms;
+              best[0] = g;
+              best[1] = sp;
+              best[2] = xr;
+              best[3] = ln;
+            }
+          }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) {
+      if (rc == MPSQ_ERR_CUDA) fail(MPSQ_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      return rc;
+    }
+  }
+  j->opt_graph = best[0];
+  j->opt_spread = best[1];
+  j->opt_xrows = best[2];
+  j->opt_lanes = best[3];
+  drop_graphs(j);
+  if (!cached && cache_path && *cache_path) {
+    if (FILE* f = fopen(cache_path, "a")) {
+      fprintf(f, "%s %d %d %d %d %.4f\n", key.c_str(), best[0], best[1], best[2], best[3], best_t);
+      fclose(f);
+    }
+  }
+  if (choice) {
+    choice[0] = best[0];
+    choice[1] = best[1];
+    choice[2] = best[2];
+    choice[3] = best[3];
+  }
+  if (best_ms) *best_ms = best_t;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_get_option(const mpsq_job* j, int option, int* value) {
+  if (!j || !value) return fail(MPSQ_ERR_ARG, "get_option: null pointer");
+  switch (option) {
+    case MPSQ_OPT_GRAPH: *value = j->opt_graph; break;
+    case MPSQ_OPT_SPREAD: *value = j->opt_spread; break;
+    case MPSQ_OPT_XROWS: *value = j->opt_xrows; break;
+    case MPSQ_OPT_LANES: *value = j->opt_lanes; break;
+    default: return fail(MPSQ_ERR_ARG, "get_option: unknown option %d", option);
+  }
+  return MPSQ_OK;
 }
 
 template <typename T>
@@ -1666,6 +1886,18 @@ extern "C" int mpsq_job_stage_ms(mpsq_job* j, double* ms4, int64_t* frames, int 
 extern "C" int mpsq_job_amplitudes(mpsq_job* j, void** cs_dev) {
   if (!j || !cs_dev) return fail(MPSQ_ERR_ARG, "amplitudes: null pointer");
   *cs_dev = j->cs;
+  return MPSQ_OK;
+}
+
+extern "C" int mpsq_job_info(const mpsq_job* j, int* width, int64_t* fine_grid, int* n_grids,
+                             int* pruned, int* lanes) {
+  if (!j) return fail(MPSQ_ERR_ARG, "job_info: null job");
+  if (width) *width = j->es.w;
+  if (fine_grid)
+    for (int k = 0; k < 3; ++k) fine_grid[k] = j->g.nf[k];
+  if (n_grids) *n_grids = j->sa.ngrid;
+  if (pruned) *pruned = j->pruned ? 1 : 0;
+  if (lanes) *lanes = j->lane2 ? 2 : 1;
   return MPSQ_OK;
 }
 

@@ -329,7 +329,7 @@ int launch_scan(const int* counts, int* starts, int64_t n, cudaStream_t s);
 template <typename T>
 int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,
-                  typename Cplx<T>::type* fine, cudaStream_t s);
+                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core = true);
 
 // Tensor-core spreading of packed real species pairs (3D, 16^3 tiles, FP32 grid); strengths
 // must be real with |s| <= 8.  Selected by default; MPSQ_SPREAD=fma in the environment keeps

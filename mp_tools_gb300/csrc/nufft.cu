@@ -44,10 +44,8 @@ EsKernel es_params(double eps, int precision) {
   if (eps > 1e-1) eps = 1e-1;
   int w = (int)std::ceil(std::log10(1.0 / eps)) + 1;
   w = std::max(2, std::min(16, w));
-  // FP32 transforms use the width of eps = 1e-6 whatever eps asks for: about the accuracy FP32
-  // spreading and FFTs reach (relative l2 ~2e-6), and the width at which every FP32 kernel
-  // path (tensor-core and CUDA-core spreading, 2D and 3D) is parity-tested on the GPU.
-  if (precision != MPSQ_FP64) w = 7;
+  // FP32 transforms stop at eps = 1e-7 (w = 8): below that the FP32 rounding of spreading and
+  // FFT, not the kernel's truncation, sets the error.
   EsKernel k;
   k.w = w;
   k.beta = 2.30 * w;
@@ -548,10 +546,11 @@ template <typename T, int DIM, int NT>
 static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                               const int* idx, const typename Cplx<T>::type* cv, int64_t c_stride,
                               const int* starts, int nkeys, int ntrans, bool real_pair,
-                              typename Cplx<T>::type* fine, cudaStream_t s) {
+                              typename Cplx<T>::type* fine, cudaStream_t s,
+                              bool tensor_core = true) {
   if constexpr (std::is_same<T, float>::value && DIM == 3) {
     if (a.tile[0] == 16 && a.tile[1] == 16 && a.tile[2] == 16 && a.w >= 3 && a.w <= 8) {
-      if (real_pair && spread_pair_mma_enabled())
+      if (real_pair && tensor_core && spread_pair_mma_enabled())
         return launch_spread_pair_mma(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
       dim3 grid((unsigned)nkeys, (unsigned)ntrans);
       const int rp = real_pair ? 1 : 0;
@@ -589,19 +588,19 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
 template <typename T>
 int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,
-                  typename Cplx<T>::type* fine, cudaStream_t s) {
+                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core) {
   constexpr int NT = sizeof(T) == 4 ? 256 : 128;
   int nkeys = (int)(a.n_tiles * a.ngrid);
   if (a.dim == 3)
     return launch_spread_impl<T, 3, NT>(a, recs, nullptr, str, 0, starts, nkeys, 1, real_pair,
-                                        fine, s);
+                                        fine, s, tensor_core);
   return launch_spread_impl<T, 2, NT>(a, recs, nullptr, str, 0, starts, nkeys, 1, real_pair,
-                                      fine, s);
+                                      fine, s, tensor_core);
 }
 template int launch_spread<float>(const SpreadArgs&, const RecF*, const float2*, const int*, bool,
-                                  float2*, cudaStream_t);
+                                  float2*, cudaStream_t, bool);
 template int launch_spread<double>(const SpreadArgs&, const RecD*, const double2*, const int*,
-                                   bool, double2*, cudaStream_t);
+                                   bool, double2*, cudaStream_t, bool);
 
 int make_fft_plan(const GridGeom& g, int ngrid, int precision, cudaStream_t s, cufftHandle* h) {
   long long n[3];
@@ -861,11 +860,12 @@ extern "C" const char* mpsq_version(void) { return "mpsq 0.1 (sm_103a)"; }
 extern "C" int64_t mpsq_launch_count(void) { return mpsq::g_launches.load(); }
 
 // ====================================================== allocation-free 2D type-1 entry point
-// For callers that may not allocate device memory (code running while a CUDA graph is being
-// captured, hosts whose device memory is handed out by their own pool, or plug-in hosts that
-// forbid allocation inside a call): all scratch of this transform — fine grid, bin counts and
-// offsets, point records, correction factors, error flag — lives in one file-scope device
-// array that every GPU loading this library holds until the process exits.
+// For callers that may not allocate device memory during a call (hosts whose device memory is
+// handed out by their own pool under a fixed budget, or plug-in hosts that forbid allocation
+// inside a call): all scratch of this transform — fine grid, bin counts and offsets, point
+// records, correction factors, error flag — lives in one file-scope device array that every
+// GPU loading this library holds until the process exits.  Nothing is copied from host memory;
+// the call ends by reading the error flag back and synchronising the stream.
 namespace {
 
 constexpr int64_t kNoallocMaxPoints = 65536;   // nonuniform points per call
@@ -898,6 +898,57 @@ int64_t pow2_at_least(int64_t n) {
   int64_t p = 1;
   while (p < n) p <<= 1;
   return p;
+}
+
+constexpr int kNoallocMaxQuad = 4 * 16 + 40;   // Gauss-Legendre order for the widest kernel
+
+// Deconvolution factors 1/phihat(k) of both axes, computed on the device into the scratch (the
+// quadrature of es_correction: Gauss-Legendre nodes by Newton iteration on P_n, then
+// phihat(k) = int_{-w/2}^{w/2} phi(2u/w) cos(2 pi k u / nf) du), so that a call copies nothing
+// from host memory.  One CTA; corr2 (the unused third axis) is set to 1.
+__global__ void noalloc_corr_kernel(int w, double beta, int64_t nf0, int64_t ms, int64_t nf1,
+                                    int64_t mt, double* __restrict__ corr0,
+                                    double* __restrict__ corr1, double* __restrict__ corr2) {
+  __shared__ double su[kNoallocMaxQuad], sf[kNoallocMaxQuad];
+  const int nq = 4 * w + 40;
+  const double half = 0.5 * w;
+  for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+    double z = cospi((i + 0.75) / (nq + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= nq; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = nq * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= nq; ++k) {
+      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = nq * (z * p1 - p0) / (z * z - 1.0);
+    const double wt = 2.0 / ((1.0 - z * z) * dp * dp);
+    su[i] = half * z;
+    sf[i] = half * wt * exp(beta * (sqrt(fmax(0.0, 1.0 - z * z)) - 1.0));
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < ms + mt; i += blockDim.x) {
+    const bool first = i < ms;
+    const int64_t m = first ? ms : mt, nf = first ? nf0 : nf1;
+    const int64_t ii = first ? i : i - ms;
+    const double k = (double)(ii - m / 2);
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) s += sf[q] * cospi(2.0 * k * su[q] / (double)nf);
+    (first ? corr0 : corr1)[ii] = 1.0 / s;
+  }
+  if (threadIdx.x == 0) *corr2 = 1.0;
 }
 
 }  // namespace
@@ -975,14 +1026,10 @@ extern "C" int mpsq_nufft2d1_noalloc(int64_t nj, const double* x, const double* 
   double* corr1 = (double*)take(sizeof(double) * mt);
   double* corr2 = (double*)take(sizeof(double));
   int* err = (int*)take(sizeof(int));
-  // deconvolution factors (host quadrature, copied into the scratch)
-  std::vector<double> h0(ms), h1(mt);
-  const double one = 1.0;
-  es_correction(es, nf0, ms, h0.data());
-  es_correction(es, nf1, mt, h1.data());
-  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr0, h0.data(), sizeof(double) * ms, cudaMemcpyHostToDevice, s));
-  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr1, h1.data(), sizeof(double) * mt, cudaMemcpyHostToDevice, s));
-  MPSQ_CUDA_TRY(cudaMemcpyAsync(corr2, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+  // deconvolution factors, computed on the device (no copy from host memory)
+  if (es.w > 16) return fail(MPSQ_ERR_ARG, "nufft2d1_noalloc: kernel width %d above 16", es.w);
+  noalloc_corr_kernel<<<1, 128, 0, s>>>(es.w, es.beta, nf0, ms, nf1, mt, corr0, corr1, corr2);
+  MPSQ_LAUNCH_CHECK();
   // the previous call's contents stay in the array: clear what must start at zero
   MPSQ_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
   MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (a.n_tiles + 1), s));

@@ -399,6 +399,44 @@ class SqomJob:
             self._h, first, count, int(j_plane), int(round(float(g.n_bz))), float(g.q_min[0]),
             float(g.q_min[1]), C.c_void_p(base.ctypes.data)), "transform_onephonon")
 
+    def info(self) -> dict:
+        """Spreading width, fine-grid lengths, number of fine grids per frame, whether the
+        pruned three-pass transform runs, and the number of frame lanes."""
+        w, ng, pr, ln = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        nf = (C.c_int64 * 3)()
+        check(_lib.load().mpsq_job_info(self._h, C.byref(w), nf, C.byref(ng), C.byref(pr),
+                                        C.byref(ln)), "info")
+        return {"width": w.value, "fine_grid": tuple(nf), "n_grids": ng.value,
+                "pruned": bool(pr.value), "lanes": ln.value}
+
+    def n_grids(self) -> int:
+        return self.info()["n_grids"]
+
+    def set_option(self, option: int, value: int):
+        """Run-time choice (_lib.OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES); see mpsq.h."""
+        check(_lib.load().mpsq_job_set_option(self._h, int(option), int(value)), "set_option")
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int()
+        check(_lib.load().mpsq_job_get_option(self._h, int(option), C.byref(v)), "get_option")
+        return v.value
+
+    def autotune(self, first: int = 0, count: int | None = None, cache: str | None = None) -> dict:
+        """Times the transform of frames [first, first + count) under every applicable
+        combination of run-time choices, keeps the fastest (see mpsq_job_autotune); cache: a
+        file of recorded choices per job shape."""
+        count = min(self.n_frames - first, 8) if count is None else count
+        ch = (C.c_int * 4)()
+        ms = C.c_double()
+        check(_lib.load().mpsq_job_autotune(self._h, int(first), int(count),
+                                            cache.encode() if cache else None, ch, C.byref(ms)),
+              "autotune")
+        return {"graph": ch[0], "spread": ("tensor-core", "cuda-core")[ch[1]], "xrows": ch[2],
+                "lanes": ch[3], "ms_per_call": ms.value, "frames_per_call": count}
+
+    def uses_pruned_fft(self) -> bool:
+        return self.info()["pruned"]
+
     def sync(self):
         self._flush_outputs()
         check(_lib.load().mpsq_job_sync(self._h), "sync")
@@ -504,6 +542,28 @@ class SqomJob:
         check_rt(cudart.cudaMemcpy(C.c_void_p(out.data_ptr()), C.c_void_p(src), C.c_size_t(nbytes), 2),
                  "cudaMemcpy")
         return out.numpy().reshape(self.n_frames, -1)
+
+    def amplitudes_device(self):
+        """cs(t,Q) as a torch tensor (n_frames, n_Q) viewing the job's device store (no copy;
+        valid until the job is closed, rewritten by the next transform)."""
+        import torch
+        dt = "<c16" if self.precision == _lib.FP64 else "<c8"
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (self.n_frames, self.grid.n_modes), "typestr": dt,
+                                        "data": (self.amplitudes_ptr(), False), "version": 3}
+
+        self.sync()
+        return torch.as_tensor(_View(), device="cuda")
+
+    def amplitudes_at(self, q_index, frames=None) -> np.ndarray:
+        """cs(t, Q) at the given flat Q indices (all frames, or the given frame indices), gathered
+        on the device and copied to the host: (n_t, len(q_index))."""
+        import torch
+        cs = self.amplitudes_device()
+        q = torch.as_tensor(np.asarray(q_index, np.int64), device="cuda")
+        sel = cs if frames is None else cs[torch.as_tensor(np.asarray(frames, np.int64), device="cuda")]
+        return sel[:, q].cpu().numpy()
 
     def norm2(self) -> float:
         return float(sum(self.species_counts)) ** 2

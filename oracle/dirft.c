@@ -118,6 +118,65 @@ void oracle_dirft_modes(int dim, int64_t nj, const double* x, const double* y, c
   }
 }
 
+/* Selected modes, for large point sets: per point, the phase factors of every mode index along
+ * each axis (phase_row, recomputed exactly every 16 steps), then the product of the three axis
+ * factors per selected mode.  kq holds nq triples inside [kmin[a], kmin[a] + span[a]).  Points
+ * are split over threads, each accumulating its own partial sums; the partials are added in
+ * thread order. */
+void oracle_dirft_modes_tab(int dim, int64_t nj, const double* x, const double* y, const double* z,
+                            const double* c, int iflag, int64_t nq, const int64_t* kq,
+                            const int64_t* kmin, const int64_t* span, double* out) {
+  const double s = iflag >= 0 ? 1.0 : -1.0;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  double* part = (double*)calloc((size_t)nt * 2 * (size_t)nq, sizeof(double));
+  if (!part) return;
+#pragma omp parallel
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    double* acc = part + (size_t)t * 2 * (size_t)nq;
+    double* tab[3][2];
+    for (int a = 0; a < 3; ++a) {
+      tab[a][0] = (double*)malloc(sizeof(double) * (size_t)(span[a] > 0 ? span[a] : 1));
+      tab[a][1] = (double*)malloc(sizeof(double) * (size_t)(span[a] > 0 ? span[a] : 1));
+    }
+#pragma omp for schedule(static)
+    for (int64_t j = 0; j < nj; ++j) {
+      const double pos[3] = {x[j], y[j], dim == 3 ? z[j] : 0.0};
+      for (int a = 0; a < dim; ++a) phase_row(pos[a], s, kmin[a], span[a], tab[a][0], tab[a][1]);
+      const double cr = c[2 * j], ci = c[2 * j + 1];
+      for (int64_t q = 0; q < nq; ++q) {
+        const int64_t i0 = kq[3 * q] - kmin[0], i1 = kq[3 * q + 1] - kmin[1];
+        double er = tab[0][0][i0] * tab[1][0][i1] - tab[0][1][i0] * tab[1][1][i1];
+        double ei = tab[0][0][i0] * tab[1][1][i1] + tab[0][1][i0] * tab[1][0][i1];
+        if (dim == 3) {
+          const int64_t i2 = kq[3 * q + 2] - kmin[2];
+          const double fr = er * tab[2][0][i2] - ei * tab[2][1][i2];
+          ei = er * tab[2][1][i2] + ei * tab[2][0][i2];
+          er = fr;
+        }
+        acc[2 * q] += cr * er - ci * ei;
+        acc[2 * q + 1] += cr * ei + ci * er;
+      }
+    }
+    for (int a = 0; a < 3; ++a) {
+      free(tab[a][0]);
+      free(tab[a][1]);
+    }
+  }
+  for (int64_t q = 0; q < 2 * nq; ++q) {
+    double v = 0.0;
+    for (int t = 0; t < nt; ++t) v += part[(size_t)t * 2 * (size_t)nq + q];
+    out[q] = v;
+  }
+  free(part);
+}
+
 /* CPU exponential-of-semicircle spreading onto an n0 x n1 x n2 periodic grid (interleaved
  * complex, x fastest, zeroed by the caller).  g: 3*nj grid coordinates already folded to
  * [0, n).  Kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)) on w cells per axis.
