@@ -1508,6 +1508,7 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
     float2* const b1 = odd ? j->b1_2 : j->b1;
     const float4* frame = j->traj + (size_t)t * j->d.n_atoms_frame;
     if (mark(0)) return MPSQ_ERR_CUDA;
+    PhaseRange bin_range("mpsq:sort");
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
       job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, starts,
@@ -1523,10 +1524,14 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
       MPSQ_LAUNCH_CHECK();
     }
     if (mark(1)) return MPSQ_ERR_CUDA;
+    nvtxRangePop();                       // end of mpsq:sort
+    nvtxRangePushA("mpsq:spread");
     rc = launch_spread<T>(a, (const R*)recs, (const C*)str, starts, j->pa.pack != 0, (C*)fine, s,
                           j->opt_spread == 0);
     if (rc) return rc;
     if (mark(2)) return MPSQ_ERR_CUDA;
+    nvtxRangePop();                       // end of mpsq:spread
+    nvtxRangePushA("mpsq:fft+deconv");    // popped by bin_range at the end of the frame
     C* csf = (C*)j->cs + (size_t)t * nm;
     C* css = j->cs_species ? (C*)j->cs_species + (size_t)t * j->d.n_species * nm : nullptr;
     bool done = false;

@@ -3,12 +3,25 @@
 
 #include <cuda_runtime.h>
 #include <cufft.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
 
 #include "../../include/mpsq.h"
+
+namespace mpsq {
+// Host-side NVTX range around the launches of one pipeline phase (sort/bin, spread, fft +
+// deconvolution, time transform, reduction), so that a profiler can select a phase's kernels.
+// Header-only NVTX: without an attached tool a push/pop costs a few nanoseconds.
+struct PhaseRange {
+  explicit PhaseRange(const char* name) { nvtxRangePushA(name); }
+  ~PhaseRange() { nvtxRangePop(); }
+  PhaseRange(const PhaseRange&) = delete;
+  PhaseRange& operator=(const PhaseRange&) = delete;
+};
+}  // namespace mpsq
 
 namespace mpsq {
 

@@ -64,12 +64,14 @@ struct MmaSmem {
 
 // The ES kernel value of cell i of a support, phi(z) = exp(beta (sqrt(1 - z^2) - 1)) at
 // z = (2 (u + i) - W) / W, u in [0, 1) the point's offset inside its first cell, as a
-// polynomial of degree W + 2 in v = 2u - 1 per cell (Chebyshev interpolation on the host,
-// monomial coefficients, Horner on the FMA pipe; no exp/sqrt on the special-function unit).
-// The interpolation error is below the kernel's own edge value e^-beta (about eps / 10).
+// polynomial in v = 2u - 1 per cell (Chebyshev interpolation on the host, monomial
+// coefficients, Horner on the FMA pipe; no exp/sqrt on the special-function unit).  Degree
+// W + 2 up to width 6, 8 at width 7, W from width 8 on: the lowest degrees whose FP32 Horner
+// evaluation error (below 1e-7 of the kernel's peak, set by FP32 rounding) is no larger than
+// that of W + 2.
 template <int W>
 struct EsPoly {
-  static constexpr int kDeg = W + 2;
+  static constexpr int kDeg = W >= 8 ? W : (W == 7 ? 8 : W + 2);
   float c[W][kDeg + 1];   // c[i][k]: coefficient of v^k for cell i
 };
 

@@ -568,6 +568,7 @@ using namespace mpsq;
 
 extern "C" int mpsq_job_sq_total(mpsq_job* j, double norm2, float* out, int host) {
   if (!j) return fail(MPSQ_ERR_ARG, "sq_total: null job");
+  PhaseRange range("mpsq:reduce");
   JobView v = job_view(j);
   OutBuf b;
   int rc = out_prepare(out, host, v.n_q, &b);
@@ -699,6 +700,7 @@ int dispersion_impl(mpsq_job* j, const SeriesArgs& src, int32_t n_int, const flo
 extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wind,
                                    int32_t j_freq, const float* q2_norm, double scale,
                                    float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst: null pointer");
   return econst_impl(j, weighted_series(job_view(j)), n_int, t_wind, j_freq, q2_norm, scale, out,
                      host);
@@ -707,6 +709,7 @@ extern "C" int mpsq_job_sqw_econst(mpsq_job* j, int32_t n_int, const float* t_wi
 extern "C" int mpsq_job_sqw_econst_pair(mpsq_job* j, int32_t n_int, const float* t_wind,
                                         int32_t j_freq, int32_t sp1, int32_t sp2, double scale,
                                         float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j || !t_wind) return fail(MPSQ_ERR_ARG, "sqw_econst_pair: null pointer");
   SeriesArgs src;
   const int rc = pair_series(job_view(j), sp1, sp2, "sqw_econst_pair", &src);
@@ -718,6 +721,7 @@ extern "C" int mpsq_job_sqw_dispersion(mpsq_job* j, int32_t n_int, const float* 
                                        int32_t n_path, const int64_t* q_index, int32_t n_freq,
                                        const float* q2_norm, double scale, float* out,
                                        int host) {
+  PhaseRange range("mpsq:time");
   if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion: null pointer");
   return dispersion_impl(j, weighted_series(job_view(j)), n_int, t_wind, n_path, q_index, n_freq,
                          q2_norm, scale, out, host);
@@ -727,6 +731,7 @@ extern "C" int mpsq_job_sqw_dispersion_pair(mpsq_job* j, int32_t n_int, const fl
                                             int32_t n_path, const int64_t* q_index,
                                             int32_t n_freq, int32_t sp1, int32_t sp2,
                                             double scale, float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j || !t_wind || !q_index) return fail(MPSQ_ERR_ARG, "sqw_dispersion_pair: null pointer");
   SeriesArgs src;
   const int rc = pair_series(job_view(j), sp1, sp2, "sqw_dispersion_pair", &src);
@@ -737,6 +742,7 @@ extern "C" int mpsq_job_sqw_dispersion_pair(mpsq_job* j, int32_t n_int, const fl
 
 extern "C" int mpsq_job_iqt(mpsq_job* j, int32_t n_int, int32_t lag, const float* q2_norm,
                             double scale, float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j) return fail(MPSQ_ERR_ARG, "iqt: null job");
   JobView v = job_view(j);
   if (n_int < 1 || lag < 0 || lag + n_int > v.n_frames)
@@ -777,6 +783,7 @@ extern "C" int mpsq_job_iqt(mpsq_job* j, int32_t n_int, int32_t lag, const float
 extern "C" int mpsq_job_iqt_dispersion(mpsq_job* j, int32_t n_int, int32_t n_path,
                                        const int64_t* q_index, const float* q2_norm,
                                        double scale, float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j || !q_index) return fail(MPSQ_ERR_ARG, "iqt_dispersion: null pointer");
   JobView v = job_view(j);
   if (n_int < 1 || n_int > v.n_frames || n_path < 1)
@@ -818,6 +825,7 @@ extern "C" int mpsq_job_iqt_dispersion(mpsq_job* j, int32_t n_int, int32_t n_pat
 
 extern "C" int mpsq_job_sqw_gauss(mpsq_job* j, double fwhm_frames, int32_t n_freq,
                                   const float* q2_norm, double scale, float* out, int host) {
+  PhaseRange range("mpsq:time");
   if (!j) return fail(MPSQ_ERR_ARG, "sqw_gauss: null job");
   JobView v = job_view(j);
   const int nt = v.n_frames;

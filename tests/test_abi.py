@@ -1,6 +1,8 @@
 """The C-ABI library loads and exports every entry point include/mpsq.h declares (no GPU)."""
 import re
 import subprocess
+
+import pytest
 from pathlib import Path
 
 from conftest import ROOT
@@ -75,14 +77,7 @@ def test_injected_allocation_failure_reports_err_alloc(lib, monkeypatch):
     assert b"job_create" in (msg if isinstance(msg, bytes) else msg.encode())
 
 
-def test_c_caller_of_the_fortran_entry_points(lib, tmp_path):
-    """tests/abi_harness.c, compiled as C against include/mpsq.h and linked to libmpsq, calls
-    finufft2d1_ / finufft3d1_ with gfortran's by-reference convention.  On a machine with a
-    GPU the modes equal the FP64 direct sum (column-major, k1 fastest); without one every call
-    reports MPSQ_ERR_CUDA in ier, a null scalar MPSQ_ERR_ARG, and the first failure is
-    printed once to stderr (the reference never reads ier)."""
-    import numpy as np
-    import oracle
+def _run_harness(tmp_path):
     from mp_tools_gb300 import build as mbuild
     so = Path(mbuild.LIB)
     exe = tmp_path / "abi_harness"
@@ -94,19 +89,46 @@ def test_c_caller_of_the_fortran_entry_points(lib, tmp_path):
     assert run.returncode == 0, run.stderr
     rows = {ln.split()[0]: ln.split()[1:] for ln in run.stdout.splitlines()}
     ier = {k: int(v[0].split("=")[1]) for k, v in rows.items()}
-    assert ier["null"] == 1
+    return run, rows, ier
+
+
+def _check_harness_modes(rows):
+    import numpy as np
+    import oracle
     x, y, z = [0.1, -1.2, 2.5], [-2.0, 0.7, 3.0], [1.5, -0.3, -3.1]
     c = np.array([1.0, 0.5 - 0.5j, -1.0 + 2.0j])
+    got = np.array([float(v) for v in rows["2d"][1:]]).view(np.complex128)
+    want = oracle.dirft2d1(x, y, c, -1, 4, 3).ravel()
+    assert np.abs(got - want).max() < 1e-7 * np.abs(want).max()
+    got3 = np.array([float(v) for v in rows["3d"][1:]]).view(np.complex128)
+    want3 = oracle.dirft3d1(x, y, z, c, -1, 4, 3, 2).ravel()
+    assert np.abs(got3 - want3).max() < 1e-7 * np.abs(want3).max()
+
+
+def test_c_caller_of_the_fortran_entry_points(lib, tmp_path):
+    """tests/abi_harness.c, compiled as C against include/mpsq.h and linked to libmpsq, calls
+    finufft2d1_ / finufft3d1_ with gfortran's by-reference convention.  On a machine with a
+    GPU the modes equal the FP64 direct sum (column-major, k1 fastest); without one every call
+    reports MPSQ_ERR_CUDA in ier, a null scalar MPSQ_ERR_ARG, and the first failure is
+    printed once to stderr (the reference never reads ier)."""
+    run, rows, ier = _run_harness(tmp_path)
+    assert ier["null"] == 1
     if ier["2d"] == 0:
-        got = np.array([float(v) for v in rows["2d"][1:]]).view(np.complex128)
-        want = oracle.dirft2d1(x, y, c, -1, 4, 3).ravel()
-        assert np.abs(got - want).max() < 1e-7 * np.abs(want).max()
-        got3 = np.array([float(v) for v in rows["3d"][1:]]).view(np.complex128)
-        want3 = oracle.dirft3d1(x, y, z, c, -1, 4, 3, 2).ravel()
-        assert np.abs(got3 - want3).max() < 1e-7 * np.abs(want3).max()
+        _check_harness_modes(rows)
     else:
         assert ier["2d"] == 3 and ier["3d"] == 3
         assert run.stderr.count("mpsq: finufft replacement failed") == 1
+
+
+@pytest.mark.gpu
+def test_c_caller_of_the_fortran_entry_points_on_gpu(lib, cuda, tmp_path):
+    """The same C caller on a GPU: both calls succeed (ier = 0), the modes equal the FP64
+    direct sum, the null-scalar call reports MPSQ_ERR_ARG and only that failure is printed."""
+    run, rows, ier = _run_harness(tmp_path)
+    assert ier["2d"] == 0 and ier["3d"] == 0, run.stderr
+    _check_harness_modes(rows)
+    assert ier["null"] == 1
+    assert run.stderr.count("mpsq: finufft replacement failed") == 1
 
 
 def test_job_memory_estimate_structure(lib):
