@@ -538,26 +538,37 @@ def run_profile_case(args):
 
 
 def run_serving(args):
-    """Serving stream (C3 shape, scaled so that it finishes in about a minute): ABO3 jobs with
-    Poisson arrivals, edge / frames / zones uniform in the given ranges, FP32 at eps 1e-5,
-    through the request server (continuous batching, admission by device memory), then the
-    same jobs one at a time in FP64 on a bounded subset.  One JSON line with p50/p99 latency,
+    """Serving stream: ABO3 jobs with Poisson arrivals, edge / frames / zones uniform in the
+    given ranges, FP32 at eps 1e-5, through the request server (continuous batching, admission
+    by device memory, jobs larger than the budget run by Q slabs), then the same kind of jobs
+    one at a time in FP64 on a bounded subset (the smallest).  --serving-c3 takes the serving
+    configuration's own ranges (edge 16-100 cells, 1-256 frames, 4-8 zones) with plane-wave
+    trajectories made on the device at admission; the default is a scaled-down mix with host
+    trajectories.  The offered rate is --serving-load x the capacity measured on the first
+    --serving-capacity-jobs jobs submitted at once.  One JSON line with p50/p99 latency,
     throughput and the completed / rejected / queued counts."""
     import torch
     from mp_tools_gb300 import _lib, serve
     import dataclasses
+    if args.serving_c3:
+        args.serving_edge, args.serving_frames, args.serving_zones = "16,100", "1,256", "4,8"
     edge = tuple(int(x) for x in args.serving_edge.split(","))
     frames = tuple(int(x) for x in args.serving_frames.split(","))
     zones = tuple(int(x) for x in args.serving_zones.split(","))
+    dev = bool(args.serving_c3)
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(args.serving_budget_frac * free)
     reqs = serve.poisson_stream(args.serving_jobs, 1.0, SEED + 3, edge=edge, frames=frames,
-                                zones=zones)
+                                zones=zones, device_frames=dev)
     warm = serve.poisson_stream(2, 100.0, SEED + 4, edge=(edge[0], edge[0]), frames=(4, 4),
-                                zones=(zones[0], zones[0]))
-    serve.Server(max_active=args.serving_slots).run(warm)          # builds, pools, streams
+                                zones=(zones[0], zones[0]), device_frames=dev)
+    serve.Server(budget_bytes=budget, max_active=args.serving_slots, keep_results=False).run(warm)
     torch.cuda.synchronize()
-    # capacity: the whole stream at once; then Poisson arrivals at load x capacity
-    _, cap = serve.Server(max_active=args.serving_slots).run(
-        [dataclasses.replace(r, arrival=0.0) for r in reqs])
+    # capacity: the first jobs of the stream at once; then Poisson arrivals at load x capacity
+    k = args.serving_capacity_jobs or len(reqs)
+    cap_reqs = [dataclasses.replace(r, arrival=0.0) for r in reqs[:k]]
+    _, cap = serve.Server(budget_bytes=budget, max_active=args.serving_slots,
+                          keep_results=False).run(cap_reqs)
     capacity = cap["nu_pts_per_s"]
     rate = args.serving_load * capacity / float(np.mean([r.nu_points for r in reqs]))
     if args.serving_rate > 0:
@@ -565,32 +576,42 @@ def run_serving(args):
     rng = np.random.default_rng(SEED + 5)
     t = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
     reqs = [dataclasses.replace(r, arrival=float(a)) for r, a in zip(reqs, t)]
-    srv = serve.Server(max_active=args.serving_slots)
+    srv = serve.Server(budget_bytes=budget, max_active=args.serving_slots, keep_results=False)
     res, st = srv.run(reqs)
-    # the baseline of the config: one job at a time in FP64 (a bounded subset)
-    sub = reqs[: args.serving_fp64_jobs]
+    slabbed = sum(1 for r in reqs if getattr(r, "_q_slab", 0))
+    # the baseline of the config: one job at a time in FP64 (the smallest jobs of the stream)
+    sub = sorted(reqs, key=lambda r: r.nu_points * r.grid.n_modes)[: args.serving_fp64_jobs]
     plain = [serve.Request(r.rid, 0.0, r.frames, r.counts, r.grid,
-                           dict(r.job_kwargs, precision=_lib.FP64)) for r in sub]
+                           dict(r.job_kwargs, precision=_lib.FP64), t_step=r.t_step) for r in sub]
     t0 = time.perf_counter()
-    serve.Server(max_active=1).run(plain)
+    serve.Server(budget_bytes=budget, max_active=1, keep_results=False).run(plain)
     t_fp64 = time.perf_counter() - t0
     pts_sub = sum(r.nu_points for r in sub)
+    t0 = time.perf_counter()
+    serve.Server(budget_bytes=budget, max_active=1, keep_results=False).run(
+        [dataclasses.replace(r, arrival=0.0) for r in sub])
+    t_fp32_sub = time.perf_counter() - t0
+    kind = ("plane-wave trajectories made on the device at admission" if dev
+            else "Gaussian displacements, host trajectories")
     out = {"metric": "job latency p50/p99 (s), serving stream", "impl": "mpsq",
-           "unit": "s", "data": "synthetic (seeded ABO3 supercells, Gaussian displacements)",
-           "config": {"workload": f"{len(reqs)} ABO3 jobs, Poisson arrivals at {rate:.1f} /s "
+           "unit": "s", "data": f"synthetic (seeded ABO3 supercells, {kind})",
+           "config": {"workload": f"{len(reqs)} ABO3 jobs, Poisson arrivals at {rate:.3g} /s "
                                   f"(offered load {args.serving_load:g} x the measured capacity "
                                   f"{capacity:.3g} NU pts/s), edge {edge}, frames {frames}, "
                                   f"zones {zones}, FP32 eps 1e-5, neutron weights, S(Q) + "
                                   f"up to 4 E=const maps per job",
-                      "slots": args.serving_slots, "budget_bytes": st["budget_bytes"]},
+                      "slots": args.serving_slots, "budget_bytes": st["budget_bytes"],
+                      "capacity_jobs": k},
            "capacity_nu_pts_s": capacity, "capacity_p50_s": cap["p50_s"],
            "capacity_p99_s": cap["p99_s"],
            "p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"],
            "throughput_nu_pts_s": st["nu_pts_per_s"], "wall_s": st["wall_s"],
            "completed": st["completed"], "rejected": st["rejected"], "queued": st["queued"],
            "max_queue": st["max_queue"], "peak_admitted_bytes": st["peak_admitted_bytes"],
+           "jobs_run_by_q_slabs": slabbed,
            "fp64_one_at_a_time": {"jobs": len(sub), "nu_pts_s": pts_sub / t_fp64,
-                                  "wall_s": t_fp64}}
+                                  "wall_s": t_fp64,
+                                  "fp32_same_jobs_one_at_a_time_nu_pts_s": pts_sub / t_fp32_sub}}
     print(json.dumps(out), flush=True)
 
 
@@ -1144,6 +1165,13 @@ def main():
     ap.add_argument("--serving-zones", default="2,4")
     ap.add_argument("--serving-slots", type=int, default=8)
     ap.add_argument("--serving-fp64-jobs", type=int, default=6)
+    ap.add_argument("--serving-c3", action="store_true",
+                    help="the serving configuration's own ranges (edge 16-100, 1-256 frames, "
+                         "4-8 zones), trajectories made on the device")
+    ap.add_argument("--serving-budget-frac", type=float, default=0.8,
+                    help="device memory budget of the server, as a fraction of the free memory")
+    ap.add_argument("--serving-capacity-jobs", type=int, default=0,
+                    help="jobs of the capacity measurement (0: all)")
     args = ap.parse_args()
     if args.eps is not None:
         global EPS, EPS_CFG

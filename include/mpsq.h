@@ -164,6 +164,11 @@ typedef struct mpsq_job_desc {
                                 memory pool), so creating and destroying a job never waits
                                 for the device (concurrent jobs of a request server); one
                                 frame lane.  0: plain allocation, destroy waits for the job */
+  int64_t q_slab;            /* 0: the amplitude store holds every Q mode.  > 0 (3D only): it
+                                holds a slab of at most q_slab kz planes (n_qx n_qy q_slab
+                                modes per frame), chosen by mpsq_job_set_q_slab; transforms
+                                and maps then cover that slab (jobs whose full store would not
+                                fit in device memory run slab by slab)                      */
 } mpsq_job_desc;
 
 typedef struct mpsq_job mpsq_job;
@@ -284,6 +289,14 @@ int mpsq_job_transform_onephonon(mpsq_job* job, int32_t first, int32_t count, in
 
 /* Synchronise the job's stream. */
 int mpsq_job_sync(mpsq_job* job);
+
+/* Q slab of a job created with q_slab > 0 (no reference counterpart: the reference keeps the
+ * whole store, code/src/mp_sqom56.f90:963): kz planes [z0, z0 + min(q_slab, n_qz - z0)).  The
+ * next transforms store the amplitudes of those planes only, and the maps (total S(Q), E=const,
+ * Gaussian spectrum, I(Q,t), dispersion cuts with slab-local indices) cover the slab, their
+ * outputs holding n_qx n_qy (planes of the slab) values with Q index x fastest from plane z0.
+ * Asynchronous (host state only); the radial histogram needs the whole store. */
+int mpsq_job_set_q_slab(mpsq_job* job, int64_t z0);
 
 /* Run-time choices of a job (no reference counterpart; FINUFFT's opts play this role).  Any
  * change drops the job's captured graphs.

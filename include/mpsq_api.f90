@@ -47,6 +47,7 @@ module mpsq_api
     integer(c_int32_t) :: no_pack
     integer(c_int32_t) :: no_pruned_fft
     integer(c_int32_t) :: stream_ordered
+    integer(c_int64_t) :: q_slab
   end type
 
   public :: mpsq_job_create, mpsq_job_destroy, mpsq_job_estimate_bytes, mpsq_job_set_frames, &

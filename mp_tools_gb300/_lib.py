@@ -31,7 +31,7 @@ EXPORTS = [
     "mpsq_job_sqw_econst", "mpsq_job_sqw_dispersion", "mpsq_job_sqw_econst_pair",
     "mpsq_job_sqw_dispersion_pair", "mpsq_job_iqt", "mpsq_job_iqt_dispersion",
     "mpsq_job_sqw_gauss", "mpsq_job_sync", "mpsq_job_info", "mpsq_job_set_option",
-    "mpsq_job_get_option", "mpsq_job_autotune",
+    "mpsq_job_get_option", "mpsq_job_autotune", "mpsq_job_set_q_slab",
     "mpsq_job_profile", "mpsq_job_stage_ms", "mpsq_job_radial_hist", "mpsq_last_error",
     "mpsq_version", "mpsq_launch_count",
     "mpsq_nufft2d1_noalloc", "mpsq_speckle_filter", "mpsq_job_transform_onephonon",
@@ -74,6 +74,7 @@ class JobDesc(C.Structure):
         ("no_pack", C.c_int32),
         ("no_pruned_fft", C.c_int32),
         ("stream_ordered", C.c_int32),
+        ("q_slab", C.c_int64),
     ]
 
 
@@ -130,6 +131,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "mpsq_job_set_option": (C.c_int, [vp, C.c_int, C.c_int]),
         "mpsq_job_get_option": (C.c_int, [vp, C.c_int, vp]),
         "mpsq_job_autotune": (C.c_int, [vp, i32, i32, C.c_char_p, vp, vp]),
+        "mpsq_job_set_q_slab": (C.c_int, [vp, i64]),
         "mpsq_job_profile": (C.c_int, [vp, C.c_int]),
         "mpsq_job_stage_ms": (C.c_int, [vp, vp, vp, C.c_int]),
         "mpsq_job_radial_hist": (C.c_int, [vp, vp, vp, dbl, dbl, i32, dbl, vp, C.c_int]),

@@ -1,8 +1,11 @@
 // Link-compatible replacements of FINUFFT's type-1 entry points, the boundary MP_TOOLS calls
 // at code/src/mp_sqom56.f90:1148 (finufft2d1, once per frame and species) and
 // code/src/mp_sql56.f90:1129 (once per z-layer).  Host arrays in and out; the call is
-// synchronous and retains no caller pointer.  Plans and device staging buffers are cached
-// across calls (mp_sqom repeats identical (n_qx, n_qy, eps, iflag) calls for every frame).
+// synchronous and retains no caller pointer.  Plans, device buffers and pinned host staging
+// buffers are cached across calls (mp_sqom repeats identical (n_qx, n_qy, eps, iflag) calls for
+// every frame): the caller's (pageable) arrays are copied into pinned memory on the host, moved
+// by one asynchronous copy each way, and the call synchronises once, reading the modes and the
+// device error flag together.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,10 +33,12 @@ struct DropinState {
   int next = 0;
   void* dpts = nullptr;  // x, y, z staging
   size_t dpts_bytes = 0;
-  void* dc = nullptr;
-  size_t dc_bytes = 0;
   void* dfk = nullptr;
   size_t dfk_bytes = 0;
+  void* hin = nullptr;   // pinned host staging of the inputs (x, y, z, c)
+  size_t hin_bytes = 0;
+  void* hout = nullptr;  // pinned host staging of the modes, then the error flag
+  size_t hout_bytes = 0;
   bool warned = false;
 };
 
@@ -48,6 +53,16 @@ int grow(void** p, size_t* have, size_t need) {
   *p = nullptr;
   *have = 0;
   MPSQ_CUDA_TRY(cudaMalloc(p, need));
+  *have = need;
+  return MPSQ_OK;
+}
+
+int grow_pinned(void** p, size_t* have, size_t need) {
+  if (need <= *have) return MPSQ_OK;
+  cudaFreeHost(*p);
+  *p = nullptr;
+  *have = 0;
+  MPSQ_CUDA_TRY(cudaHostAlloc(p, need, cudaHostAllocDefault));
   *have = need;
   return MPSQ_OK;
 }
@@ -99,27 +114,47 @@ int run_type1(int dim, int64_t nj, const T* x, const T* y, const T* z, const T* 
   mpsq_nufft_plan* plan = nullptr;
   int rc = get_plan(st, dim, m, iflag, eps, prec, &plan);
   if (rc) return rc;
-  const size_t pb = sizeof(T) * (size_t)std::max<int64_t>(nj, 1);
-  rc = grow(&st.dpts, &st.dpts_bytes, 3 * pb);
-  if (!rc) rc = grow(&st.dc, &st.dc_bytes, 2 * pb);
-  if (!rc) rc = grow(&st.dfk, &st.dfk_bytes, 2 * sizeof(T) * (size_t)nm);
+  // inputs in one block [x | y | z | c] (z only in 3D), device and pinned host alike; every
+  // segment starts on a 256-byte boundary (the strengths are read as 8- or 16-byte complex)
+  const size_t n1 = (size_t)std::max<int64_t>(nj, 1);
+  const size_t seg = (sizeof(T) * n1 + 255) & ~size_t(255);       // one coordinate array
+  const size_t off_c = (size_t)dim * seg;
+  const size_t in_bytes = off_c + 2 * sizeof(T) * n1;
+  const size_t fk_bytes = 2 * sizeof(T) * (size_t)nm;
+  const size_t flag_off = (fk_bytes + 15) & ~size_t(15);
+  rc = grow(&st.dpts, &st.dpts_bytes, in_bytes);
+  if (!rc) rc = grow(&st.dfk, &st.dfk_bytes, fk_bytes);
+  if (!rc) rc = grow_pinned(&st.hin, &st.hin_bytes, in_bytes);
+  if (!rc) rc = grow_pinned(&st.hout, &st.hout_bytes, flag_off + sizeof(int));
   if (rc) return rc;
-  T* dx = (T*)st.dpts;
-  T* dy = dx + std::max<int64_t>(nj, 1);
-  T* dz = dy + std::max<int64_t>(nj, 1);
+  char* const dbase = (char*)st.dpts;
+  T* dx = (T*)dbase;
+  T* dy = (T*)(dbase + seg);
+  T* dz = (T*)(dbase + 2 * seg);
+  T* dc = (T*)(dbase + off_c);
   cudaStream_t s = st.stream;
   if (nj > 0) {
-    MPSQ_CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(T) * nj, cudaMemcpyHostToDevice, s));
-    MPSQ_CUDA_TRY(cudaMemcpyAsync(dy, y, sizeof(T) * nj, cudaMemcpyHostToDevice, s));
-    if (dim == 3) MPSQ_CUDA_TRY(cudaMemcpyAsync(dz, z, sizeof(T) * nj, cudaMemcpyHostToDevice, s));
-    MPSQ_CUDA_TRY(cudaMemcpyAsync(st.dc, c, 2 * sizeof(T) * nj, cudaMemcpyHostToDevice, s));
+    char* const hbase = (char*)st.hin;
+    memcpy(hbase, x, sizeof(T) * nj);
+    memcpy(hbase + seg, y, sizeof(T) * nj);
+    if (dim == 3) memcpy(hbase + 2 * seg, z, sizeof(T) * nj);
+    memcpy(hbase + off_c, c, 2 * sizeof(T) * nj);
+    MPSQ_CUDA_TRY(cudaMemcpyAsync(dbase, hbase, in_bytes, cudaMemcpyHostToDevice, s));
   }
   rc = mpsq_nufft_setpts(plan, nj, dx, dy, dim == 3 ? dz : nullptr);
-  if (!rc) rc = mpsq_nufft_execute(plan, st.dc, st.dfk);
+  if (!rc) rc = mpsq_nufft_execute(plan, dc, st.dfk);
   if (rc) return rc;
-  MPSQ_CUDA_TRY(cudaMemcpyAsync(fk, st.dfk, 2 * sizeof(T) * nm, cudaMemcpyDeviceToHost, s));
+  char* hout = (char*)st.hout;
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(hout, st.dfk, fk_bytes, cudaMemcpyDeviceToHost, s));
+  MPSQ_CUDA_TRY(cudaMemcpyAsync(hout + flag_off, plan_error_flag(plan), sizeof(int),
+                                cudaMemcpyDeviceToHost, s));
   MPSQ_CUDA_TRY(cudaStreamSynchronize(s));
-  return mpsq_nufft_check_error(plan);
+  int flag = 0;
+  memcpy(&flag, hout + flag_off, sizeof(int));
+  rc = dev_error_status(flag);
+  if (rc) return rc;
+  memcpy(fk, hout, fk_bytes);
+  return MPSQ_OK;
 }
 
 int report(int rc) {

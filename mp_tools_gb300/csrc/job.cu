@@ -171,6 +171,11 @@ struct mpsq_job {
     int64_t launches;
   };
   std::vector<Graph> graphs;  // captured frame loops, by (first, count)
+  // Q slab (q_slab > 0): the store holds kz planes [slab_z0, slab_z0 + slab_planes())
+  int64_t slab_nz = 0;
+  int64_t slab_z0 = 0;
+  int64_t slab_planes() const { return slab_nz ? std::min(slab_nz, g.m[2] - slab_z0) : g.m[2]; }
+  int64_t store_modes() const { return g.m[0] * g.m[1] * slab_planes(); }
 };
 
 // Device memory of a job: stream-ordered (from the device's memory pool, on the job's stream)
@@ -434,9 +439,10 @@ __device__ __forceinline__ T species_weight(const WeightArgs& w, int s, T s2) {
 }
 
 // Deconvolution, pair separation, species weighting; writes cs(t, Q) for one frame.
-// Grid: x over the m0 modes of a row, y over the m1*m2 rows (32-bit index math).
+// Grid: x over the m0 modes of a row, y over the m1 rows, z over the nz planes z0.. of the
+// store's Q slab (the whole grid: z0 = 0, nz = m2; 32-bit index math).
 template <typename T>
-__global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
+__global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2, int z0, int nz,
                                   const typename Cplx<T>::type* __restrict__ fine,
                                   const T* __restrict__ c0, const T* __restrict__ c1,
                                   const T* __restrict__ c2, WeightArgs w,
@@ -445,9 +451,9 @@ __global__ void job_deconv_kernel(SpreadArgs a, int m0, int m1, int m2,
   using C = typename Cplx<T>::type;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m0) return;
-  const int j = blockIdx.y, l = blockIdx.z;
-  const int row = l * m1 + j;
-  const int64_t nm = (int64_t)m0 * m1 * m2;
+  const int j = blockIdx.y, l = z0 + (int)blockIdx.z;   // kz plane of the slab
+  const int row = (int)blockIdx.z * m1 + j;               // row of the store
+  const int64_t nm = (int64_t)m0 * m1 * nz;
   const int64_t q = (int64_t)row * m0 + i;
   const int kx = i - m0 / 2, ky = j - m1 / 2, kz = l - m2 / 2;
   const int nf0 = (int)a.nf[0], nf1 = (int)a.nf[1], nf2 = (int)a.nf[2];
@@ -850,7 +856,8 @@ __device__ __forceinline__ float2 zpass_mode(float2 G, float2 Gm, bool pair, int
 template <int N>
 __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     fftz_dif_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
-                           int h0, int h1, int h2, int ngroups, const float2* __restrict__ gtw,
+                           int z0, int nz, int h0, int h1, int h2, int ngroups,
+                           const float2* __restrict__ gtw,
                            const float* __restrict__ c0, const float* __restrict__ c1,
                            const float* __restrict__ c2, WeightArgs w,
                            float2* __restrict__ cs_frame, float2* __restrict__ cs_species_frame) {
@@ -864,7 +871,7 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   const int x0 = blockIdx.x * T, iy = blockIdx.y;
   const int iym = 2 * h1 - iy;
   const bool mrow = iym < m1 && iym != iy;              // this CTA also forms the row iym
-  const int64_t nm = (int64_t)m0 * m1 * m2;
+  const int64_t nm = (int64_t)m0 * m1 * nz;              // modes per frame in the store
   copy_twiddles<N>(tw, gtw);
   float4 acc[OUTS], accm[OUTS];
 #pragma unroll
@@ -906,7 +913,8 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     for (int p = 0; p < OUTS; ++p) {
       const int e = tid + 256 * p;
       const int c = 2 * (e % TP), iz = e / TP;
-      if (iz >= m2 || x0 + c >= K0) continue;
+      const int lz = iz - z0;                            // plane within the store's Q slab
+      if (iz >= m2 || lz < 0 || lz >= nz || x0 + c >= K0) continue;
       const int fz = iz - h2;
       const int pf = dif_position<N>(wrap_freq(fz, N)), pm = dif_position<N>(wrap_freq(-fz, N));
       const float4 P2 = *reinterpret_cast<const float4*>(&xs[pf * L + c]);
@@ -929,13 +937,13 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
         float2 a = make_float2(0.f, 0.f);
         if (x < m0)
           a = zpass_mode(P, Mm, pair, sa, sb, c0[x] * cy * cz, x - h0, ky, fz, w,
-                         ((int64_t)iz * m1 + iy) * m0 + x, nm, cs_species_frame);
+                         ((int64_t)lz * m1 + iy) * m0 + x, nm, cs_species_frame);
         // M mode (iym, 2h0 - x, iz): G(k) on the M line, G(-k) on the P line at -fz
         float2 b = make_float2(0.f, 0.f);
         const int xm = 2 * h0 - x;
         if (mrow && xm < m0)
           b = zpass_mode(M, Pm, pair, sa, sb, c0[xm] * cym * cz, xm - h0, kym, fz, w,
-                         ((int64_t)iz * m1 + iym) * m0 + xm, nm, cs_species_frame);
+                         ((int64_t)lz * m1 + iym) * m0 + xm, nm, cs_species_frame);
         if (hv) {
           acc[p].z += a.x;
           acc[p].w += a.y;
@@ -954,13 +962,13 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   for (int p = 0; p < OUTS; ++p) {
     const int e = tid + 256 * p;
     const int c = 2 * (e % TP), iz = e / TP;
-    const int x = x0 + c;
-    if (iz >= m2 || x >= K0) continue;
-    float2* q = cs_frame + ((int64_t)iz * m1 + iy) * m0 + x;
+    const int x = x0 + c, lz = iz - z0;
+    if (iz >= m2 || lz < 0 || lz >= nz || x >= K0) continue;
+    float2* q = cs_frame + ((int64_t)lz * m1 + iy) * m0 + x;
     if (x < m0) q[0] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
     if (x + 1 < m0) q[1] = make_float2(acc[p].z * w.wnorm_f, acc[p].w * w.wnorm_f);
     if (mrow) {
-      float2* qm = cs_frame + ((int64_t)iz * m1 + iym) * m0;
+      float2* qm = cs_frame + ((int64_t)lz * m1 + iym) * m0;
       const int xm = 2 * h0 - x;   // in [0, 2 h0]; the column x + 1 mirrors to xm - 1
       if (xm < m0) qm[xm] = make_float2(accm[p].x * w.wnorm_f, accm[p].y * w.wnorm_f);
       if (x + 1 < K0 && xm - 1 < m0) qm[xm - 1] = make_float2(accm[p].z * w.wnorm_f, accm[p].w * w.wnorm_f);
@@ -976,6 +984,7 @@ struct PruneLaunch {
   int n[3], m[3], h[3], K[3];
   int ngrid, ngroups;
   int xrows = kPassLinesX;   // rows per CTA of the X pass (4 or 8)
+  int z0 = 0, nz = 0;        // kz planes of the store's Q slab
   const float2* tw[3];
   const float* c[3];
   cudaStream_t s;
@@ -1018,7 +1027,8 @@ static int launch_prune_z(const PruneLaunch& p, const WeightArgs& w, float2* csf
   const int rows = std::min(p.m[1], p.h[1] + 1);   // ky rows iy <= h1; each also forms 2 h1 - iy
   // x tiles cover the K0 = 2 h0 + 1 kept columns: column 2 h0 is the mirror of mode column 0
   fftz_dif_deconv_kernel<N><<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)rows), 256, sm, p.s>>>(
-      p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.h[0], p.h[1], p.h[2], p.ngroups, p.tw[2],
+      p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.z0, p.nz, p.h[0], p.h[1], p.h[2], p.ngroups,
+      p.tw[2],
       p.c[0], p.c[1], p.c[2], w, csf, css);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
@@ -1069,6 +1079,8 @@ static int job_layout(const mpsq_job_desc* d, EsKernel* es, GridGeom* g, int* ng
     if (d->species_offset[s + 1] < d->species_offset[s])
       return fail(MPSQ_ERR_ARG, "job: species offsets not increasing");
   if (d->weight_mode < 1 || d->weight_mode > 3) return fail(MPSQ_ERR_ARG, "job: bad weight_mode");
+  if (d->q_slab < 0 || (d->q_slab > 0 && d->ndim != 3))
+    return fail(MPSQ_ERR_ARG, "job: q_slab must be 0, or > 0 for a 3D job");
   *es = es_params(d->eps, d->precision);
   int rc = make_geom(d->ndim, d->n_modes, es->w, g);
   if (rc) return rc;
@@ -1154,9 +1166,11 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
   b += d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision));
   b += (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8;
   b += d->n_atoms_frame * 4 + (int64_t)(std::max(1, ng) * g.n_tiles + 2) * 8;  // locality order
-  b += (int64_t)d->n_frames * g.n_modes * (int64_t)csize(d->precision);     // cs(t,Q)
+  const int64_t store = d->q_slab > 0 ? g.m[0] * g.m[1] * std::min<int64_t>(d->q_slab, g.m[2])
+                                      : g.n_modes;                      // modes per frame kept
+  b += (int64_t)d->n_frames * store * (int64_t)csize(d->precision);     // cs(t,Q)
   if (d->store_species)
-    b += (int64_t)d->n_frames * d->n_species * g.n_modes * (int64_t)csize(d->precision);
+    b += (int64_t)d->n_frames * d->n_species * store * (int64_t)csize(d->precision);
   bool pruned = d->precision == MPSQ_FP32 && d->ndim == 3 && !d->no_pruned_fft;
   for (int k = 0; k < 3 && pruned; ++k) pruned = fft_size_compiled((int)g.nf[k]);
   if (pruned) {  // X-pass output, plus a second frame lane (fine grid, bins, records, X output)
@@ -1323,8 +1337,10 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   A((void**)&j->perm_starts, sizeof(int) * (nkeys + 2));
   A(&j->recs, (size_t)j->cap * rsize(prec));
   A(&j->str, (size_t)j->cap * cs);
-  A(&j->cs, (size_t)d->n_frames * j->g.n_modes * cs);
-  if (d->store_species) A(&j->cs_species, (size_t)d->n_frames * d->n_species * j->g.n_modes * cs);
+  j->slab_nz = d->q_slab > 0 ? std::min<int64_t>(d->q_slab, j->g.m[2]) : 0;
+  const int64_t store = j->store_modes();
+  A(&j->cs, (size_t)d->n_frames * store * cs);
+  if (d->store_species) A(&j->cs_species, (size_t)d->n_frames * d->n_species * store * cs);
   A((void**)&j->err, sizeof(int));
   for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
     std::vector<double> c(j->g.m[k], 1.0);
@@ -1463,7 +1479,7 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
   const int64_t nkeys = (int64_t)a.ngrid * a.n_tiles;
   const int bt = 256;
   const unsigned nb = (unsigned)((j->d.n_atoms_frame + bt - 1) / bt);
-  const int64_t nm = j->g.n_modes;
+  const int64_t nm = j->store_modes();
   const bool prof = j->profile;
   auto mark = [&](int k) -> int {
     if (prof) MPSQ_CUDA_TRY(cudaEventRecord(j->ev[k], s));
@@ -1553,6 +1569,8 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
         pl.ngrid = a.ngrid;
         pl.ngroups = j->ngroups;
         pl.xrows = j->opt_xrows;
+        pl.z0 = (int)j->slab_z0;
+        pl.nz = (int)j->slab_planes();
         pl.s = s;
         rc = run_pruned(pl, j->wa, (float2*)csf, (float2*)css, prof ? j->ev[3] : nullptr);
         if (rc) return rc;
@@ -1563,9 +1581,11 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
       rc = exec_fft(j->fft, j->d.precision, j->fine, CUFFT_FORWARD);
       if (rc) return rc;
       if (mark(3)) return MPSQ_ERR_CUDA;
-      const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1], (unsigned)j->g.m[2]);
+      const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1],
+                       (unsigned)j->slab_planes());
       job_deconv_kernel<T><<<dgrid, 128, 0, s>>>(
-          a, (int)j->g.m[0], (int)j->g.m[1], (int)j->g.m[2], (const C*)j->fine, (const T*)j->corr[0],
+          a, (int)j->g.m[0], (int)j->g.m[1], (int)j->g.m[2], (int)j->slab_z0,
+          (int)j->slab_planes(), (const C*)j->fine, (const T*)j->corr[0],
           (const T*)j->corr[1], (const T*)j->corr[2], j->wa, csf, css);
       MPSQ_LAUNCH_CHECK();
     }
@@ -1906,6 +1926,17 @@ extern "C" int mpsq_job_info(const mpsq_job* j, int* width, int64_t* fine_grid, 
   return MPSQ_OK;
 }
 
+extern "C" int mpsq_job_set_q_slab(mpsq_job* j, int64_t z0) {
+  if (!j) return fail(MPSQ_ERR_ARG, "set_q_slab: null job");
+  if (j->slab_nz == 0) return fail(MPSQ_ERR_STATE, "set_q_slab: job created without q_slab");
+  if (z0 < 0 || z0 >= j->g.m[2])
+    return fail(MPSQ_ERR_ARG, "set_q_slab: z0 = %lld outside [0, %lld)", (long long)z0,
+                (long long)j->g.m[2]);
+  j->slab_z0 = z0;
+  drop_graphs(j);   // captured graphs hold the previous slab
+  return MPSQ_OK;
+}
+
 extern "C" int mpsq_job_sync(mpsq_job* j) {
   if (!j) return fail(MPSQ_ERR_ARG, "sync: null job");
   MPSQ_CUDA_TRY(cudaStreamSynchronize(j->s));
@@ -1920,7 +1951,8 @@ JobView job_view(mpsq_job* j) {
   v.s = j->s;
   v.cs = j->cs;
   v.cs_species = j->cs_species;
-  v.n_q = j->g.n_modes;
+  v.n_q = j->store_modes();
+  v.slab = j->slab_nz > 0;
   v.n_frames = j->d.n_frames;
   v.n_species = j->d.n_species;
   for (int k = 0; k < 3; ++k) v.m[k] = j->g.m[k];

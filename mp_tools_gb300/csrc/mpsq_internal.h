@@ -360,6 +360,10 @@ int exec_fft(cufftHandle h, int precision, void* data, int direction);
 constexpr int kErrRecOverflow = 1;
 constexpr int kErrBadIndex = 2;
 int check_dev_error(const int* dev_flag, cudaStream_t s);
+// The device error flag of a plan (for callers that copy it back with their own results) and
+// the status a flag value stands for.
+const int* plan_error_flag(const mpsq_nufft_plan* p);
+int dev_error_status(int flag);
 
 // View of a job's amplitude store for the time-axis kernels.
 struct JobView {
@@ -367,7 +371,8 @@ struct JobView {
   cudaStream_t s;
   void* cs;            // n_frames x n_q complex, Q fastest
   void* cs_species;    // n_frames x n_species x n_q complex or NULL
-  int64_t n_q;
+  int64_t n_q;         // modes per frame in the store (those of the current Q slab)
+  bool slab;           // the store holds a Q slab, not the whole grid
   int32_t n_frames;
   int32_t n_species;
   int64_t m[3];        // modes per dimension

@@ -340,6 +340,103 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// One CTA owns one tile; each warp takes one record at a time.  The warp's lanes evaluate the
+// record's DIM x w kernel values together (one exponential per lane), then cover its support
+// with rows of w cells along x (32 / w rows per pass), so that the shared-memory atomics of one
+// instruction all go to distinct cells.  Points that coincide — the atoms of a crystal column
+// projected onto a Q plane, the case of mp_sqom's (hk0) maps — then no longer make the 32 lanes
+// of a warp add to the same cell at once, which the thread-per-record form above serialises.
+template <typename T, int DIM, int NT>
+__global__ void __launch_bounds__(NT)
+    spread_tile_warp_kernel(SpreadArgs a, const typename RecOf<T>::type* __restrict__ recs,
+                            const int* __restrict__ idx,
+                            const typename Cplx<T>::type* __restrict__ cv, int64_t c_stride,
+                            const int* __restrict__ starts, int real_pair,
+                            typename Cplx<T>::type* __restrict__ fine) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int TX = a.tile[0], TY = a.tile[1], TZ = a.tile[2];
+  const int cells = TX * TY * TZ;
+  const int w = a.w;
+  T* acc_re = reinterpret_cast<T*>(smem_raw);
+  T* acc_im = acc_re + cells;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T* ker = acc_im + cells + warp * 48;    // [axis][16]: this warp's record's kernel values
+  const int64_t key = blockIdx.x;
+  const int trans = blockIdx.y;
+  const int64_t keygrid = key / a.n_tiles;
+  const int64_t tile = key - keygrid * a.n_tiles;
+  const int tx = (int)(tile % a.ntile[0]);
+  const int ty = (int)((tile / a.ntile[0]) % a.ntile[1]);
+  const int tz = (int)(tile / ((int64_t)a.ntile[0] * a.ntile[1]));
+  for (int c = tid; c < cells; c += NT) {
+    acc_re[c] = (T)0;
+    acc_im[c] = (T)0;
+  }
+  __syncthreads();
+  const T beta = (T)a.beta;
+  const T two_over_w = (T)(2.0 / w);
+  const int rows = 32 / w;                 // support rows per pass (w <= 16)
+  const int li = lane % w, lj = lane / w;  // lanes with lj >= rows stay idle
+  const int r0 = starts[key], r1 = starts[key + 1];
+  for (int r = r0 + warp; r < r1; r += NT / 32) {
+    const auto rec = recs[r];              // one address for the whole warp
+    C c;
+    if (cv) {
+      c = idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r];
+    } else {
+      c.x = (T)1;
+      c.y = (T)0;
+    }
+    for (int l = lane; l < DIM * w; l += 32) {   // DIM w <= 48 values
+      const int ax = l / w, i = l - ax * w;
+      const T d = ax == 0 ? rec.dx : (ax == 1 ? rec.dy : rec.dz);
+      ker[ax * 16 + i] = es_eval<T>((d + (T)i) * two_over_w, beta);
+    }
+    __syncwarp();
+    const int lx = (rec.packed & 0xff) - 64;
+    const int ly = ((rec.packed >> 8) & 0xff) - 64;
+    const int lz = ((rec.packed >> 16) & 0xff) - 64;
+    const int comp = (rec.packed >> 24) & 1;
+    const int x = lx + li;
+    const bool xin = lj < rows && x >= 0 && x < TX;
+    const T kx = ker[li];
+    const int nzs = DIM == 3 ? w : 1;
+    for (int kz = 0; kz < nzs; ++kz) {
+      const int z = DIM == 3 ? lz + kz : 0;
+      if (DIM == 3 && (z < 0 || z >= TZ)) continue;        // warp-uniform
+      const T vz = DIM == 3 ? ker[32 + kz] : (T)1;
+      for (int j0 = 0; j0 < w; j0 += rows) {
+        const int j = j0 + lj, y = ly + j;
+        if (xin && j < w && y >= 0 && y < TY) {
+          const T v = kx * ker[16 + j] * vz;
+          const int cell = (z * TY + y) * TX + x;
+          if (real_pair) {
+            atomicAdd(&(comp ? acc_im : acc_re)[cell], v * c.x);
+          } else {
+            atomicAdd(&acc_re[cell], v * c.x);
+            atomicAdd(&acc_im[cell], v * c.y);
+          }
+        }
+      }
+    }
+    __syncwarp();                          // ker is rewritten by the warp's next record
+  }
+  __syncthreads();
+  C* out = fine + (keygrid + trans) * a.n_fine;
+  const int64_t nf0 = a.nf[0], nf1 = a.nf[1];
+  const int64_t x0 = (int64_t)tx * TX, y0 = (int64_t)ty * TY, z0 = (int64_t)tz * TZ;
+  for (int c = tid; c < cells; c += NT) {
+    const int x = c % TX;
+    const int y = (c / TX) % TY;
+    const int z = c / (TX * TY);
+    C v;
+    v.x = acc_re[c];
+    v.y = acc_im[c];
+    out[((z0 + z) * nf1 + (y0 + y)) * nf0 + (x0 + x)] = v;
+  }
+}
+
 // FP32, 3D, 16^3 tiles, compile-time kernel width W, no atomics: thread (x, y) of the CTA owns
 // the 16-cell z-column (x, y, 0..15) of the tile in registers.  Records are staged in shared
 // memory in chunks with their x and y kernel values and their z kernel row already shifted
@@ -566,6 +663,25 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
       return MPSQ_OK;
     }
   }
+  dim3 grid((unsigned)nkeys, (unsigned)ntrans);
+  if (a.w <= 16 && (DIM == 2 || sizeof(T) == 8)) {
+    // warp per record: 2D grids (crystal columns coincide on a Q plane) and FP64 volumes
+    constexpr int NTW = 256;
+    const size_t smem = (2 * (size_t)a.tile[0] * a.tile[1] * a.tile[2] + (NTW / 32) * 48) * sizeof(T);
+    static std::once_flag once_w;
+    static cudaError_t attr_w = cudaSuccess;
+    std::call_once(once_w, [&] {
+      attr_w = cudaFuncSetAttribute(spread_tile_warp_kernel<T, DIM, NTW>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (attr_w != cudaSuccess)
+      return fail(MPSQ_ERR_CUDA, "spread smem attribute: %s", cudaGetErrorString(attr_w));
+    if (smem > 200 * 1024) return fail(MPSQ_ERR_ARG, "spread tile needs %zu B shared memory", smem);
+    spread_tile_warp_kernel<T, DIM, NTW><<<grid, NTW, smem, s>>>(a, recs, idx, cv, c_stride,
+                                                                starts, real_pair ? 1 : 0, fine);
+    MPSQ_LAUNCH_CHECK();
+    return MPSQ_OK;
+  }
   size_t smem = spread_smem<T>(a, NT);
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -576,7 +692,6 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
   if (attr_err != cudaSuccess)
     return fail(MPSQ_ERR_CUDA, "spread smem attribute: %s", cudaGetErrorString(attr_err));
   if (smem > 200 * 1024) return fail(MPSQ_ERR_ARG, "spread tile needs %zu B shared memory", smem);
-  dim3 grid((unsigned)nkeys, (unsigned)ntrans);
   spread_tile_kernel<T, DIM, NT><<<grid, NT, smem, s>>>(a, recs, idx, cv, c_stride, starts,
                                                         real_pair ? 1 : 0, fine);
   MPSQ_LAUNCH_CHECK();
@@ -849,6 +964,15 @@ extern "C" int mpsq_nufft_info(const mpsq_nufft_plan* p, int* width, int64_t* fi
     for (int k = 0; k < 3; ++k) fine_grid[k] = p->g.nf[k];
   return MPSQ_OK;
 }
+
+namespace mpsq {
+const int* plan_error_flag(const mpsq_nufft_plan* p) { return p ? p->err : nullptr; }
+int dev_error_status(int flag) {
+  if (flag & kErrRecOverflow) return fail(MPSQ_ERR_DEVICE, "binning: record capacity exceeded");
+  if (flag & kErrBadIndex) return fail(MPSQ_ERR_DEVICE, "kernel bound check failed (flag %d)", flag);
+  return MPSQ_OK;
+}
+}  // namespace mpsq
 
 extern "C" int mpsq_nufft_check_error(mpsq_nufft_plan* p) {
   if (!p) return fail(MPSQ_ERR_ARG, "null plan");

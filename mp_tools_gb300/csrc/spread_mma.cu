@@ -135,11 +135,19 @@ __device__ __forceinline__ uint32_t pack_f16x2(float first, float second) {
 
 __device__ __forceinline__ void mma_16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
                                           uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+               "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Four 8x8 f16 matrices from shared memory (ldmatrix): lane i gives the address of row i % 8 of
+// matrix i / 8 (16 bytes); r[q] receives row lane / 4, columns 2 (lane % 4) .. +1 of matrix q.
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* row_addr) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(row_addr);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
 }
 
 // Split f16 A fragment (hi, lo) of plane p for the K-block starting at slot `first`:
@@ -171,19 +179,25 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
     const bool use0 = p0 >= zlo && p0 <= zhi;
     const bool use1 = p0 + 1 >= zlo && p0 + 1 <= zhi;
     if (!use0 && !use1) continue;                       // warp-uniform
-    uint32_t bh[2][2], bl[2][2];
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      bh[nt][0] = sm.kxh[nt * 8 + g][kb * 8 + t];
-      bh[nt][1] = sm.kxh[nt * 8 + g][kb * 8 + 4 + t];
-      bl[nt][0] = sm.kxl[nt * 8 + g][kb * 8 + t];
-      bl[nt][1] = sm.kxl[nt * 8 + g][kb * 8 + 4 + t];
+    // B fragments of both n-tiles (hi and lo) by ldmatrix: matrix q = lane / 8 covers x rows
+    // (q / 2) * 8 .. +7 and records (q % 2) * 8 .. +7 of the K-block; the four registers are
+    // b0, b1 of n-tile 0 and b0, b1 of n-tile 1
+    uint32_t bh4[4], bl4[4];
+    {
+      const int lane = 4 * g + t, q = lane >> 3, r = lane & 7;
+      const int row = (q >> 1) * 8 + r, col = kb * 8 + (q & 1) * 4;   // u32 column (f16 pairs)
+      ldmatrix_x4(bh4, &sm.kxh[row][col]);
+      ldmatrix_x4(bl4, &sm.kxl[row][col]);
     }
+    const uint32_t bh[2][2] = {{bh4[0], bh4[1]}, {bh4[2], bh4[3]}};
+    const uint32_t bl[2][2] = {{bl4[0], bl4[1]}, {bl4[2], bl4[3]}};
     const float2 yA0 = *reinterpret_cast<const float2*>(&sm.ky[g][first + 2 * t]);
     const float2 yA1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t]);
     const float2 yB0 = *reinterpret_cast<const float2*>(&sm.ky[g][first + 2 * t + 8]);
     const float2 yB1 = *reinterpret_cast<const float2*>(&sm.ky[g + 8][first + 2 * t + 8]);
-    if (use0 && use1) {   // both planes: four independent accumulator chains, interleaved
+    // each product term is issued to every accumulator chain before the next term, so that
+    // consecutive MMAs are independent (the smallest terms first)
+    if (use0 && use1) {   // both planes: four independent accumulator chains
       uint32_t ah0[4], al0[4], ah1[4], al1[4];
       build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah0, al0);
       build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah1, al1);
@@ -191,8 +205,14 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
       for (int nt = 0; nt < 2; ++nt) {
         mma_16816(acc[0][nt], al0, bh[nt][0], bh[nt][1]);
         mma_16816(acc[1][nt], al1, bh[nt][0], bh[nt][1]);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
         mma_16816(acc[0][nt], ah0, bl[nt][0], bl[nt][1]);
         mma_16816(acc[1][nt], ah1, bl[nt][0], bl[nt][1]);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
         mma_16816(acc[0][nt], ah0, bh[nt][0], bh[nt][1]);
         mma_16816(acc[1][nt], ah1, bh[nt][0], bh[nt][1]);
       }
@@ -200,20 +220,20 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
       uint32_t ah[4], al[4];
       build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah, al);
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
-        mma_16816(acc[0][nt], al, bh[nt][0], bh[nt][1]);
-        mma_16816(acc[0][nt], ah, bl[nt][0], bl[nt][1]);
-        mma_16816(acc[0][nt], ah, bh[nt][0], bh[nt][1]);
-      }
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[0][nt], al, bh[nt][0], bh[nt][1]);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[0][nt], ah, bl[nt][0], bl[nt][1]);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[0][nt], ah, bh[nt][0], bh[nt][1]);
     } else {
       uint32_t ah[4], al[4];
       build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah, al);
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
-        mma_16816(acc[1][nt], al, bh[nt][0], bh[nt][1]);
-        mma_16816(acc[1][nt], ah, bl[nt][0], bl[nt][1]);
-        mma_16816(acc[1][nt], ah, bh[nt][0], bh[nt][1]);
-      }
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[1][nt], al, bh[nt][0], bh[nt][1]);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[1][nt], ah, bl[nt][0], bl[nt][1]);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) mma_16816(acc[1][nt], ah, bh[nt][0], bh[nt][1]);
     }
   }
 }

@@ -970,6 +970,7 @@ extern "C" int mpsq_job_radial_hist(mpsq_job* j, const double* a_cell_inv, const
                                     double amp_scale, double* out, int host) {
   if (!j || !a_cell_inv || !d_q || !out) return fail(MPSQ_ERR_ARG, "radial_hist: null pointer");
   JobView v = job_view(j);
+  if (v.slab) return fail(MPSQ_ERR_STATE, "radial_hist: needs the whole Q store (job has a q_slab)");
   if (n_hist < 1 || !(q_step > 0)) return fail(MPSQ_ERR_ARG, "radial_hist: bad bins");
   const void* amps = v.cs;
   int S = 1, s_stride = 1;

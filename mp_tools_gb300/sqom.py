@@ -196,9 +196,11 @@ class SqomJob:
                  ff_convention: int = _lib.FF_MP_SQOM, mask=None, window: bool = False,
                  phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
                  no_pruned_fft: bool = False, n_atoms_frame: int | None = None,
-                 use_range: bool = False, eps_x: float = 0.1, stream_ordered: bool = False):
+                 use_range: bool = False, eps_x: float = 0.1, stream_ordered: bool = False,
+                 q_slab: int = 0):
         """The job descriptor (mpsq_job_desc) of these arguments, without creating the job
-        (for estimate_bytes and admission control)."""
+        (for estimate_bytes and admission control).  q_slab > 0 (3D): the amplitude store
+        holds at most q_slab kz planes at a time (see set_q_slab)."""
         counts = [int(n) for n in species_counts]
         S = len(counts)
         if S < 1 or S > _lib.MAX_SPECIES:
@@ -253,6 +255,7 @@ class SqomJob:
         # device memory from the stream-ordered pool: creating and closing the job never wait
         # for the device (many concurrent jobs, as in the request server)
         d.stream_ordered = int(stream_ordered)
+        d.q_slab = int(q_slab)
         return d
 
     def __init__(self, grid: QGrid, *, species_counts, n_frames: int, precision: int = _lib.FP32,
@@ -261,7 +264,7 @@ class SqomJob:
                  phase_rounding: bool = False, store_species: bool = False, no_pack: bool = False,
                  no_pruned_fft: bool = False,
                  n_atoms_frame: int | None = None, use_range: bool = False, eps_x: float = 0.1,
-                 stream: int | None = None, stream_ordered: bool = False):
+                 stream: int | None = None, stream_ordered: bool = False, q_slab: int = 0):
         L = _lib.load()
         self.grid = grid
         self.species_counts = [int(n) for n in species_counts]
@@ -271,8 +274,10 @@ class SqomJob:
                              phase_rounding=phase_rounding, store_species=store_species,
                              no_pack=no_pack, no_pruned_fft=no_pruned_fft,
                              n_atoms_frame=n_atoms_frame, use_range=use_range, eps_x=eps_x,
-                             stream_ordered=stream_ordered)
+                             stream_ordered=stream_ordered, q_slab=q_slab)
         self.desc = d
+        self.q_slab = min(int(q_slab), grid.n_q[2]) if q_slab else 0
+        self.slab_z0 = 0
         self.n_frames = int(n_frames)
         self.n_atoms_frame = d.n_atoms_frame
         self.precision = precision
@@ -434,6 +439,30 @@ class SqomJob:
         return {"graph": ch[0], "spread": ("tensor-core", "cuda-core")[ch[1]], "xrows": ch[2],
                 "lanes": ch[3], "ms_per_call": ms.value, "frames_per_call": count}
 
+    @property
+    def slab_planes(self) -> int:
+        """kz planes the amplitude store holds now (all of them without a q_slab)."""
+        nz = self.grid.n_q[2]
+        return min(self.q_slab, nz - self.slab_z0) if self.q_slab else nz
+
+    @property
+    def store_modes(self) -> int:
+        """Q modes per frame in the amplitude store and in every map (the current slab's)."""
+        return self.grid.n_q[0] * self.grid.n_q[1] * self.slab_planes
+
+    def set_q_slab(self, z0: int):
+        """Selects the kz planes [z0, z0 + q_slab) (clipped) for the next transforms and maps;
+        their outputs cover Q indices z0 * n_qx * n_qy onward of the full grid."""
+        check(_lib.load().mpsq_job_set_q_slab(self._h, int(z0)), "set_q_slab")
+        self.slab_z0 = int(z0)
+
+    def slabs(self):
+        """(z0, planes, first flat Q index) of every slab, in order (one slab without q_slab)."""
+        nz = self.grid.n_q[2]
+        step = self.q_slab or nz
+        plane = self.grid.n_q[0] * self.grid.n_q[1]
+        return [(z0, min(step, nz - z0), z0 * plane) for z0 in range(0, nz, step)]
+
     def uses_pruned_fft(self) -> bool:
         return self.info()["pruned"]
 
@@ -532,7 +561,7 @@ class SqomJob:
     def amplitudes(self) -> np.ndarray:
         """cs(t,Q) copied to the host, shape (n_frames, n_Q), complex64/complex128."""
         import torch
-        n = self.n_frames * self.grid.n_modes
+        n = self.n_frames * self.store_modes
         dt = torch.complex128 if self.precision == _lib.FP64 else torch.complex64
         out = torch.empty(n, dtype=dt)
         self.sync()
@@ -550,7 +579,7 @@ class SqomJob:
         dt = "<c16" if self.precision == _lib.FP64 else "<c8"
 
         class _View:
-            __cuda_array_interface__ = {"shape": (self.n_frames, self.grid.n_modes), "typestr": dt,
+            __cuda_array_interface__ = {"shape": (self.n_frames, self.store_modes), "typestr": dt,
                                         "data": (self.amplitudes_ptr(), False), "version": 3}
 
         self.sync()
@@ -572,9 +601,9 @@ class SqomJob:
         """Total S(Q) = <|cs|^2>_t / (sum N_j)^2 (:1381-1387, :1573-1574); s_trig > 0 applies
         the speckle filter before the (sum N)^2 norm (:1531-1570, plane grids)."""
         n2 = self.norm2() if normalize else 1.0
-        res, host, copy_to = self._target(out, "sq", (self.grid.n_modes,))
+        res, host, copy_to = self._target(out, "sq", (self.store_modes,))
         if res is None:
-            res = np.empty(self.grid.n_modes, f32)
+            res = np.empty(self.store_modes, f32)
         if s_trig > 0:
             self._plane_shape("speckle filter")
             check(_lib.load().mpsq_job_sq_total(self._h, 1.0, C.c_void_p(ptr(res)), int(host)), "sq_total")
@@ -615,9 +644,9 @@ class SqomJob:
             self._plane_shape("speckle filter")
         else:
             scale *= post
-        res, host, copy_to = self._target(out, "econst", (self.grid.n_modes,))
+        res, host, copy_to = self._target(out, "econst", (self.store_modes,))
         if res is None:
-            res = np.empty(self.grid.n_modes, f32)
+            res = np.empty(self.store_modes, f32)
         L = _lib.load()
         if atom_pair is None:
             check(L.mpsq_job_sqw_econst(self._h, taxis.n_int, C.c_void_p(ptr(w)), j_freq,
@@ -669,7 +698,7 @@ class SqomJob:
         if s_trig > 0:
             self._plane_shape("speckle filter")
         scale = 1.0 if s_trig > 0 else post
-        res = np.empty(self.grid.n_modes, f32)
+        res = np.empty(self.store_modes, f32)
         check(_lib.load().mpsq_job_iqt(self._h, int(n_int), int(lag), C.c_void_p(ptr(q2)), scale,
                                        C.c_void_p(ptr(res)), 1), "iqt")
         return self._speckle(res, s_trig, False, post) if s_trig > 0 else res
@@ -700,9 +729,9 @@ class SqomJob:
         if normalize:
             scale *= t_step / self.norm2()
         q2 = None if q2_norm is None else np.ascontiguousarray(q2_norm, f32)
-        res, host, copy_to = self._target(out, "sqw", (n_freq, self.grid.n_modes))
+        res, host, copy_to = self._target(out, "sqw", (n_freq, self.store_modes))
         if res is None:
-            res = np.empty((n_freq, self.grid.n_modes), f32)
+            res = np.empty((n_freq, self.store_modes), f32)
         check(_lib.load().mpsq_job_sqw_gauss(self._h, float(fwhm), n_freq, C.c_void_p(ptr(q2)),
                                              scale, C.c_void_p(ptr(res)), int(host)), "sqw_gauss")
         if copy_to is not None:

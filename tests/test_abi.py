@@ -49,7 +49,7 @@ def test_job_descriptor_bindings_match_the_header():
     """The ctypes mirror and the Fortran bind(C) type list the C struct's members in order."""
     from mp_tools_gb300 import _lib
     members = _c_struct_members()
-    assert members[0] == "ndim" and members[-1] == "stream_ordered"
+    assert members[0] == "ndim" and members[-1] == "q_slab"
     assert [f[0] for f in _lib.JobDesc._fields_] == members
     f90 = (ROOT / "include" / "mpsq_api.f90").read_text()
     typ = f90[f90.index("type, bind(C), public :: mpsq_job_desc_t"):f90.index("end type")]

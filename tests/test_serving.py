@@ -168,3 +168,26 @@ def test_gpu_results_same_alone_and_in_the_mix(cuda):
         job.close()
     assert np.linalg.norm(mixed[2].sq - sq) <= 1e-5 * np.linalg.norm(sq)
     assert _lib.load().mpsq_launch_count() > 0
+
+
+@pytest.mark.gpu
+def test_gpu_job_larger_than_the_budget_runs_by_q_slabs(cuda):
+    """A request whose whole amplitude store does not fit in the budget is admitted with the
+    largest kz slab that does and runs slab by slab; its S(Q) and E=const maps equal those of
+    the same job with the whole store (relative l2 1e-5)."""
+    rng = np.random.default_rng(11)
+    r = serve.abo3_request(0, 0.0, 8, 8, 4, rng)            # 32^3 modes, 8 frames
+    ex = serve.GpuExecutor()
+    full, slab4 = ex._bytes(r, 0), ex._bytes(r, 4)
+    assert slab4 < full
+    budget = (full + slab4) // 2
+    res, st = serve.Server(ex, budget_bytes=budget, max_active=2).run([r])
+    assert st["completed"] == 1 and st["rejected"] == 0
+    assert 4 <= r._q_slab < r.grid.n_q[2]
+    assert st["peak_admitted_bytes"] <= budget
+    whole = serve.Request(1, 0.0, r.frames, r.counts, r.grid, r.job_kwargs)
+    ref, st2 = serve.Server(serve.GpuExecutor(), budget_bytes=4 * full, max_active=1).run([whole])
+    assert whole._q_slab == 0
+    a, b = res[0], ref[1]
+    assert np.linalg.norm(a.sq - b.sq) <= 1e-5 * np.linalg.norm(b.sq)
+    assert np.linalg.norm(a.sqw - b.sqw) <= 1e-5 * np.linalg.norm(b.sqw)
