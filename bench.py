@@ -335,6 +335,29 @@ def maps_accuracy(job, frames_dev, counts, grid, sq, sqw, fwhm, n_freq, n_q=40):
     return out
 
 
+def graph_vs_stream(job, frames):
+    """ms per frame of transform(0, frames) issued launch by launch and replayed as a captured
+    CUDA graph (each after one untimed call); the job's graph option is restored."""
+    import torch
+    from mp_tools_gb300 import _lib
+    before = job.get_option(_lib.OPT_GRAPH)
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = torch.cuda.current_stream()
+    for g in (0, 1, 0, 1):
+        job.set_option(_lib.OPT_GRAPH, g)
+        job.transform(0, frames)
+        e0.record(st)
+        for _ in range(3):
+            job.transform(0, frames)
+        e1.record(st)
+        torch.cuda.synchronize()
+        out.setdefault("graph" if g else "stream", []).append(e0.elapsed_time(e1) / (3 * frames))
+    job.set_option(_lib.OPT_GRAPH, before)
+    return {"stream_ms_per_frame": min(out["stream"]), "graph_ms_per_frame": min(out["graph"]),
+            "frames_per_call": frames}
+
+
 def error_metrics(got, ref):
     """Relative l2 errors of amplitudes and of |F|^2, and the largest relative |F|^2 error over
     the samples whose oracle |F|^2 exceeds 1e-3 of the sample maximum."""
@@ -373,6 +396,10 @@ def run_gpu(args):
     job = SqomJob(grid, species_counts=counts, n_frames=FRAMES, precision=_lib.FP32,
                   stream=stream.cuda_stream, **job_kwargs())
     job.set_frames(frames)
+    # run-time choices: graph replay vs stream-issued launches timed on 16 frames, then the
+    # autotuner's pick over graph / spreading kernel / X-pass rows / lanes (what the steps use)
+    graph_ab = graph_vs_stream(job, 16)
+    tune = job.autotune(0, 16, cache=args.tune_cache or None)
     n_freq = FRAMES // 2 + 1
     sqw = torch.empty((n_freq, grid.n_modes), dtype=torch.float32, device="cuda")
     sq = torch.empty(grid.n_modes, dtype=torch.float32, device="cuda")
@@ -456,7 +483,11 @@ def run_gpu(args):
     achieved = spread_bytes / (stage["spread"] / 1e3) / 1e9
     width = job.info()["width"]
     traffic, traffic_src = profiled_traffic(width)
-    roofline = {"bound": "hbm", "kernel": spread_kernel_name(width), "achieved": achieved,
+    kernel = (spread_kernel_name(width) if tune["spread"] == "tensor-core"
+              else f"spread3_f32_w_kernel<{width}>")
+    if tune["spread"] != "tensor-core":
+        traffic, traffic_src = None, None
+    roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": spread_bytes,
@@ -505,7 +536,8 @@ def run_gpu(args):
                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded hard-sphere Al92U8 box + Gaussian random walk)",
                "config": config_dict(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": int(launches), "clocks": clk, "accuracy": acc, "fp64_plain": fp64}
+               "gpu_launches": int(launches), "clocks": clk, "accuracy": acc, "fp64_plain": fp64,
+               "launch_forms": graph_ab, "autotune": tune}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -607,6 +639,7 @@ def run_serving(args):
            "p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"],
            "throughput_nu_pts_s": st["nu_pts_per_s"], "wall_s": st["wall_s"],
            "completed": st["completed"], "rejected": st["rejected"], "queued": st["queued"],
+           "failed": st["failed"],
            "max_queue": st["max_queue"], "peak_admitted_bytes": st["peak_admitted_bytes"],
            "jobs_run_by_q_slabs": slabbed,
            "fp64_one_at_a_time": {"jobs": len(sub), "nu_pts_s": pts_sub / t_fp64,
@@ -1150,6 +1183,7 @@ def main():
     ap.add_argument("--acc-map-q", type=int, default=40,
                     help="random Q of the S(Q) / S(Q,w) accuracy sample (all frames)")
     ap.add_argument("--eps", type=float, default=None, help="NUFFT tolerance (default: the config's)")
+    ap.add_argument("--tune-cache", default="", help="autotuner cache file (default: none)")
     ap.add_argument("--config", default="c2", choices=["c0", "c1", "c2", "c4", "dropin2d"],
                     help="workload: c2 the batched amorphous alloy (default, the headline); c0 "
                          "static FP64 ABO3 20^3; c1 inelastic ABO3 64^3 x 256 frames; c4 static "

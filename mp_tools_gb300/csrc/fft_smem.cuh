@@ -216,19 +216,73 @@ __device__ __forceinline__ void dft24(float2* v) {
   }
 }
 
+// Forward 32-point DFT in place, 8 x 4: n = 4 n1 + n2, k = k1 + 8 k2,
+// X[k] = sum_n2 W4^(n2 k2) [W32^(n2 k1) sum_n1 x[4 n1 + n2] W8^(n1 k1)].
+__device__ __forceinline__ void dft32(float2* v) {
+  // cos and sin of 2 pi m / 32, m = 0..21 (the products n2 k1 that occur)
+  const float cs[22][2] = {
+      {1.0f, 0.0f},
+      {0.98078528040323044913f, 0.19509032201612826785f},
+      {0.92387953251128675613f, 0.38268343236508977173f},
+      {0.83146961230254523708f, 0.55557023301960222474f},
+      {0.70710678118654752440f, 0.70710678118654752440f},
+      {0.55557023301960222474f, 0.83146961230254523708f},
+      {0.38268343236508977173f, 0.92387953251128675613f},
+      {0.19509032201612826785f, 0.98078528040323044913f},
+      {0.0f, 1.0f},
+      {-0.19509032201612826785f, 0.98078528040323044913f},
+      {-0.38268343236508977173f, 0.92387953251128675613f},
+      {-0.55557023301960222474f, 0.83146961230254523708f},
+      {-0.70710678118654752440f, 0.70710678118654752440f},
+      {-0.83146961230254523708f, 0.55557023301960222474f},
+      {-0.92387953251128675613f, 0.38268343236508977173f},
+      {-0.98078528040323044913f, 0.19509032201612826785f},
+      {-1.0f, 0.0f},
+      {-0.98078528040323044913f, -0.19509032201612826785f},
+      {-0.92387953251128675613f, -0.38268343236508977173f},
+      {-0.83146961230254523708f, -0.55557023301960222474f},
+      {-0.70710678118654752440f, -0.70710678118654752440f},
+      {-0.55557023301960222474f, -0.83146961230254523708f}};
+  float2 y[4][8];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    float2 a[8];
+#pragma unroll
+    for (int n1 = 0; n1 < 8; ++n1) a[n1] = v[4 * n1 + n2];
+    dft8(a);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) y[n2][k1] = a[k1];
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+    for (int k1 = 1; k1 < 8; ++k1) {
+      const int m = n2 * k1;                              // W32^m = cos - i sin
+      y[n2][k1] = cmulc(y[n2][k1], cs[m][0], -cs[m][1]);
+    }
+#pragma unroll
+  for (int k1 = 0; k1 < 8; ++k1) {
+    float2 b[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    butterfly(b, 4);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 8 * k2] = b[k2];
+  }
+}
+
 // Radices of an in-place decimation-in-frequency transform of length N = 2^a 3^b 5^c, in
-// application order.  Two stages when N = r0 r1 with r0 in {16, 24, 12, 8} and r1 in
-// {24, 16, 12, 8, 6} (fewer passes through shared memory); otherwise 8 while 8 divides what
-// remains, then 6, 4, 2, 3 or 5.
+// application order.  Two stages when N = r0 r1 with r0 in {16, 24, 12, 8, 32} and r1 in
+// {32, 24, 16, 12, 8, 6} (fewer passes through shared memory); otherwise 8 while 8 divides
+// what remains, then 6, 4, 2, 3 or 5.
 __host__ __device__ constexpr bool dif_final(int r) {
-  return r == 24 || r == 16 || r == 12 || r == 8 || r == 6;
+  return r == 32 || r == 24 || r == 16 || r == 12 || r == 8 || r == 6;
 }
 __host__ __device__ constexpr int dif_first(int N) {
   return (N % 16 == 0 && dif_final(N / 16)) ? 16
          : (N % 24 == 0 && dif_final(N / 24)) ? 24
          : (N % 12 == 0 && dif_final(N / 12)) ? 12
          : (N % 8 == 0 && dif_final(N / 8)) ? 8
-                                             : 0;
+         : (N % 32 == 0 && dif_final(N / 32)) ? 32
+                                              : 0;
 }
 __host__ __device__ constexpr int dif_greedy(int rem) {
   return rem % 8 == 0 ? 8 : rem % 6 == 0 ? 6 : rem % 4 == 0 ? 4 : rem % 2 == 0 ? 2 : rem % 3 == 0 ? 3 : 5;
@@ -254,7 +308,8 @@ __host__ __device__ constexpr int dif_block(int N, int s, int P = kDifTwoStage) 
   return b;
 }
 __device__ __forceinline__ void dft_r(float2* v, int r) {
-  if (r == 24) dft24(v);
+  if (r == 32) dft32(v);
+  else if (r == 24) dft24(v);
   else if (r == 16) dft16(v);
   else if (r == 12) dft12(v);
   else if (r == 8) dft8(v);
@@ -378,10 +433,22 @@ __device__ __forceinline__ void dif_twiddles(float2* tw) {
 }
 
 // Fine-grid lengths with compiled pruned passes: the two-stage plans (64 = 8*8, 96 = 16*6,
-// 128 = 16*8, 192 = 16*12, 256 = 16*16, 384 = 16*24) and the greedy plans 512 (8*8*8), 1024
-// (8*8*8*2) and 1152 (8*8*6*3), each exercised on the GPU by a parity test against the FP64
-// direct sum.  Other 2,3,5-smooth lengths take the cuFFT path until a parity test covers them.
-#define MPSQ_FFT_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024) X(1152)
+// 128 = 16*8, 192 = 16*12, 256 = 16*16, 384 = 16*24, 512 = 16*32, 768 = 24*32, 1024 = 32*32)
+// and greedy plans (160, 320, 640, 960, 1152, 1280, 1536, 1600), a ladder with steps of at
+// most 1.5 that covers fine grids up to 1600 points per axis (the largest a pass's shared-memory
+// tile holds); each is exercised on the GPU by a parity test against the FP64 direct sum.
+#define MPSQ_FFT_SIZES(X)                                                                    \
+  X(64) X(96) X(128) X(160) X(192) X(256) X(320) X(384) X(512) X(640) X(768) X(960) X(1024)   \
+  X(1152) X(1280) X(1536) X(1600)
+
+// The smallest compiled length >= n, or 0 above the largest.
+inline int64_t compiled_fft_size_at_least(int64_t n) {
+  int64_t best = 0;
+#define MPSQ_MIN(N) if (N >= n && (best == 0 || N < best)) best = N;
+  MPSQ_FFT_SIZES(MPSQ_MIN)
+#undef MPSQ_MIN
+  return best;
+}
 
 inline bool fft_size_compiled(int n) {
   switch (n) {

@@ -662,7 +662,7 @@ __device__ __forceinline__ int wrap_freq(int f, int n) { return f < 0 ? f + n : 
 // let more of them share an SM, so that the loads of some overlap the transforms of others.
 constexpr int kPassLinesX = 8;
 template <int N, int L>
-__global__ void __launch_bounds__(16 * L, (N <= 512 ? 48 / L : 1))
+__global__ void __launch_bounds__(16 * L, (N < 512 ? 48 / L : 1))
     fftx_dif_kernel(const float2* __restrict__ fine, int64_t n_fine, int n_rows,
                     const float2* __restrict__ gtw, int h0, int K0, float2* __restrict__ b1) {
   constexpr int NT = 16 * L, LP = L / 2, NP = N / 2;
@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(16 * L, (N <= 512 ? 48 / L : 1))
 // Pass Y: 16 consecutive x-columns (length N along y) of one z-plane per CTA; a thread moves
 // two adjacent columns.
 template <int N>
-__global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
+__global__ void __launch_bounds__(256, (N < 512 ? 3 : 1))
     ffty_dif_kernel(const float2* __restrict__ b1, int n2, int K0, const float2* __restrict__ gtw,
                     int h1, int K1, float2* __restrict__ b2) {
   constexpr int L = kPassLines, LP = L / 2;
@@ -853,7 +853,7 @@ __device__ __forceinline__ float2 zpass_mode(float2 G, float2 Gm, bool pair, int
   return make_float2(wa * G.x * corr, wa * G.y * corr);
 }
 
-template <int N>
+template <int N, bool SLAB>
 __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
     fftz_dif_deconv_kernel(const float2* __restrict__ b2, int K0, int K1, int m0, int m1, int m2,
                            int z0, int nz, int h0, int h1, int h2, int ngroups,
@@ -864,6 +864,9 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   constexpr int T = zpass_cols<N>(), L = 2 * T, LP = L / 2, TP = T / 2;
   constexpr int LOADS = (LP * N + 255) / 256, BATCH = LOADS < 8 ? LOADS : 8;
   constexpr int OUTS = (TP * (N / 2) + 255) / 256;      // column pairs x m2 (m2 <= N/2)
+  // radix-8 stages from length 512 on: the two-stage plan's radix-32 lines would not fit the
+  // register budget next to the accumulators of this pass
+  constexpr int PZ = N >= 512 ? kDifGreedy : kDifTwoStage;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* xs = reinterpret_cast<float2*>(smem_raw);     // [N][L]: T columns, then T mirrors
   float2* tw = xs + N * L;
@@ -871,7 +874,9 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   const int x0 = blockIdx.x * T, iy = blockIdx.y;
   const int iym = 2 * h1 - iy;
   const bool mrow = iym < m1 && iym != iy;              // this CTA also forms the row iym
-  const int64_t nm = (int64_t)m0 * m1 * nz;              // modes per frame in the store
+  // modes per frame in the store (SLAB: the store holds kz planes [z0, z0 + nz) only; the
+  // whole-store instantiation keeps the registers of the common case)
+  const int64_t nm = (int64_t)m0 * m1 * (SLAB ? nz : m2);
   copy_twiddles<N>(tw, gtw);
   float4 acc[OUTS], accm[OUTS];
 #pragma unroll
@@ -907,16 +912,16 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
       }
     }
     __syncthreads();
-    dif_lines<N, L>(xs, tw);
+    dif_lines<N, L, DifNoPre, PZ>(xs, tw);
     const int sa = w.sp_a[g], sb = w.sp_b[g];
 #pragma unroll
     for (int p = 0; p < OUTS; ++p) {
       const int e = tid + 256 * p;
       const int c = 2 * (e % TP), iz = e / TP;
-      const int lz = iz - z0;                            // plane within the store's Q slab
-      if (iz >= m2 || lz < 0 || lz >= nz || x0 + c >= K0) continue;
+      const int lz = SLAB ? iz - z0 : iz;                // plane within the store
+      if (iz >= m2 || (SLAB && (lz < 0 || lz >= nz)) || x0 + c >= K0) continue;
       const int fz = iz - h2;
-      const int pf = dif_position<N>(wrap_freq(fz, N)), pm = dif_position<N>(wrap_freq(-fz, N));
+      const int pf = dif_position<N, PZ>(wrap_freq(fz, N)), pm = dif_position<N, PZ>(wrap_freq(-fz, N));
       const float4 P2 = *reinterpret_cast<const float4*>(&xs[pf * L + c]);
       const float4 Pm2 = *reinterpret_cast<const float4*>(&xs[pm * L + c]);
       float4 M2 = make_float4(0.f, 0.f, 0.f, 0.f), Mm2 = M2;
@@ -962,8 +967,8 @@ __global__ void __launch_bounds__(256, (N <= 512 ? 3 : 1))
   for (int p = 0; p < OUTS; ++p) {
     const int e = tid + 256 * p;
     const int c = 2 * (e % TP), iz = e / TP;
-    const int x = x0 + c, lz = iz - z0;
-    if (iz >= m2 || lz < 0 || lz >= nz || x >= K0) continue;
+    const int x = x0 + c, lz = SLAB ? iz - z0 : iz;
+    if (iz >= m2 || (SLAB && (lz < 0 || lz >= nz)) || x >= K0) continue;
     float2* q = cs_frame + ((int64_t)lz * m1 + iy) * m0 + x;
     if (x < m0) q[0] = make_float2(acc[p].x * w.wnorm_f, acc[p].y * w.wnorm_f);
     if (x + 1 < m0) q[1] = make_float2(acc[p].z * w.wnorm_f, acc[p].w * w.wnorm_f);
@@ -1023,10 +1028,15 @@ template <int N>
 static int launch_prune_z(const PruneLaunch& p, const WeightArgs& w, float2* csf, float2* css) {
   constexpr int T = zpass_cols<N>();
   const size_t sm = pass_smem<N>(2 * T);
-  cudaFuncSetAttribute(fftz_dif_deconv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const bool slab = p.z0 != 0 || p.nz != p.m[2];
+  if (slab)
+    cudaFuncSetAttribute(fftz_dif_deconv_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  else
+    cudaFuncSetAttribute(fftz_dif_deconv_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  auto kern = slab ? fftz_dif_deconv_kernel<N, true> : fftz_dif_deconv_kernel<N, false>;
   const int rows = std::min(p.m[1], p.h[1] + 1);   // ky rows iy <= h1; each also forms 2 h1 - iy
   // x tiles cover the K0 = 2 h0 + 1 kept columns: column 2 h0 is the mirror of mode column 0
-  fftz_dif_deconv_kernel<N><<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)rows), 256, sm, p.s>>>(
+  kern<<<dim3((unsigned)((p.K[0] + T - 1) / T), (unsigned)rows), 256, sm, p.s>>>(
       p.b2, p.K[0], p.K[1], p.m[0], p.m[1], p.m[2], p.z0, p.nz, p.h[0], p.h[1], p.h[2], p.ngroups,
       p.tw[2],
       p.c[0], p.c[1], p.c[2], w, csf, css);
@@ -1084,6 +1094,20 @@ static int job_layout(const mpsq_job_desc* d, EsKernel* es, GridGeom* g, int* ng
   *es = es_params(d->eps, d->precision);
   int rc = make_geom(d->ndim, d->n_modes, es->w, g);
   if (rc) return rc;
+  if (d->precision == MPSQ_FP32 && d->ndim == 3 && !d->no_pruned_fft) {
+    // FP32 volumes: fine lengths from the compiled pruned transforms (the smallest at or above
+    // the 2,3,5-smooth length; an upsampling above 2 only lowers the kernel's error), so that
+    // every grid up to 1600 points per axis takes the pruned passes instead of cuFFT
+    for (int k = 0; k < 3; ++k) {
+      const int64_t n = compiled_fft_size_at_least(g->nf[k]);
+      if (n > 0) {
+        g->nf[k] = n;
+        g->ntile[k] = (int)(n / g->tile[k]);
+      }
+    }
+    g->n_tiles = (int64_t)g->ntile[0] * g->ntile[1] * g->ntile[2];
+    g->n_fine = g->nf[0] * g->nf[1] * g->nf[2];
+  }
   const bool qc0 = d->q_center[0] == 0.0 && d->q_center[1] == 0.0 && d->q_center[2] == 0.0;
   *pack = (qc0 && !d->no_pack) ? 1 : 0;
   int n = 0;

@@ -6,7 +6,9 @@ request is admitted as soon as an execution slot is free and its device footprin
 (``mpsq_job_estimate_bytes``: trajectory, fine grids, records, amplitude store) fits in what
 the admitted jobs leave of the budget; requests that could never fit are rejected, the others
 wait in arrival order, and a request that is still waiting when its ``max_wait`` has passed is
-cancelled without being started (an admitted job always runs to completion).  Every admitted
+cancelled without being started (an admitted job always runs to completion; one whose job
+cannot be created — a library limit its estimate did not foresee — is reported as failed and
+the stream goes on).  Every admitted
 job runs on its own CUDA stream with stream-ordered device memory, so creating and closing a
 job never waits for the device, and the kernels of jobs that are in flight together overlap on
 the GPU (a job that arrives while others run starts at once instead of after them).  The host loop only launches work, polls completion events and
@@ -230,7 +232,7 @@ class Server:
         queue: deque = deque()
         active = []                # (req, handle, bytes, admitted)
         results: dict[int, Result] = {}
-        rejected, cancelled, waited = [], [], set()
+        rejected, cancelled, failed, waited = [], [], [], set()
         used = peak = 0
         max_queue = 0
         t0 = self.clock()
@@ -278,9 +280,15 @@ class Server:
             while queue and len(active) < self.max_active and used + queue[0][1] <= self.budget:
                 r, b = queue.popleft()
                 adm = self.clock() - t0
+                try:
+                    h = self.ex.start(r)
+                except Exception as e:   # e.g. a library limit the estimate did not foresee
+                    failed.append(r.rid)
+                    self._emit({"event": "failed", "rid": r.rid, "t_s": adm, "error": str(e)})
+                    continue
                 used += b
                 peak = max(peak, used)
-                active.append((r, self.ex.start(r), b, adm))
+                active.append((r, h, b, adm))
             for r, _ in queue:            # could not start on arrival: waited for memory/slot
                 waited.add(r.rid)
             max_queue = max(max_queue, len(queue))
@@ -294,6 +302,7 @@ class Server:
         stats = {
             "completed": len(results), "rejected": len(rejected), "rejected_ids": rejected,
             "cancelled": len(cancelled), "cancelled_ids": cancelled,
+            "failed": len(failed), "failed_ids": failed,
             "queued": len(waited), "max_queue": max_queue, "budget_bytes": self.budget,
             "peak_admitted_bytes": peak, "max_active": self.max_active,
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,

@@ -1,5 +1,6 @@
 """GPU parity of the pruned three-pass fine-grid transform at every compiled fine-grid length
-against the FP64 direct sum (not against another GPU path).
+(the ladder 160 ... 1600 that FP32 volumes snap their fine grids to) against the FP64 direct sum
+(not against another GPU path).
 
 Each case is a box whose three edges give odd mode counts m = 2 nint(q L / 2 pi) + 1 with fine
 lengths (the smallest 2,3,5-smooth multiple of 16 >= 2m) chosen so that the X, the Y and the Z
@@ -20,7 +21,8 @@ pytestmark = pytest.mark.gpu
 
 Q_RANGE = 3.0
 SHORT = 31           # nint(q L / 2 pi) of a short axis: m = 63, fine length 128
-HALF_M = {192: 47, 256: 63, 384: 95, 512: 125, 1024: 255, 1152: 275}
+LENGTHS = (160, 192, 256, 320, 384, 512, 640, 768, 960, 1024, 1152, 1280, 1536, 1600)
+HALF_M = {n: (n // 2 - 2) // 2 for n in LENGTHS}   # m = n/2 - 1 or - 2: 2m rounds up to n
 
 
 def _box(half_m):
@@ -45,6 +47,7 @@ def test_pruned_length_against_direct_sum(cuda, n, axis, eps, tol):
                   n_atoms_frame=n_pts)
     try:
         assert job.uses_pruned_fft(), "fine length %d should take the pruned passes" % n
+        assert job.info()["fine_grid"][axis] == n
         job.set_frames(fr)
         job.transform()
         job.sync()

@@ -191,3 +191,29 @@ def test_gpu_job_larger_than_the_budget_runs_by_q_slabs(cuda):
     a, b = res[0], ref[1]
     assert np.linalg.norm(a.sq - b.sq) <= 1e-5 * np.linalg.norm(b.sq)
     assert np.linalg.norm(a.sqw - b.sqw) <= 1e-5 * np.linalg.norm(b.sqw)
+
+
+def test_scheduler_reports_a_job_that_fails_to_start():
+    """A request whose executor start() raises is reported as failed (with its error) and the
+    other requests of the stream still complete; its memory is not held."""
+    import io
+    import json
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    orig = ex.start
+
+    def start(req):
+        if req.rid == 1:
+            raise RuntimeError("plan creation failed")
+        return orig(req)
+
+    ex.start = start
+    reqs = [_req(0, 0.0, 60, 0.5), _req(1, 0.01, 60, 0.5), _req(2, 0.02, 60, 0.5)]
+    sink = io.StringIO()
+    res, st = serve.Server(ex, budget_bytes=130, max_active=4, clock=clk.clock, sleep=clk.sleep,
+                           metrics=sink).run(reqs)
+    assert st["failed_ids"] == [1] and st["failed"] == 1
+    assert sorted(res) == [0, 2]
+    assert res[2].admitted < 0.1             # 1's memory was never counted
+    ev = [json.loads(x) for x in sink.getvalue().splitlines()]
+    assert any(d["event"] == "failed" and "plan creation" in d["error"] for d in ev)
