@@ -335,6 +335,25 @@ def maps_accuracy(job, frames_dev, counts, grid, sq, sqw, fwhm, n_freq, n_q=40):
     return out
 
 
+def host_link(dev_in, host_in, dev_out, host_out, stream):
+    """Copy bandwidth between the host buffers of the e2e leg and the device, one copy at a time
+    (GB/s), and the time the step's transfers take at those rates when they follow each other on
+    one copy stream, as the e2e leg issues them: the floor of the e2e step."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, dst, src in (("h2d", dev_in, host_in), ("d2h", host_out, dev_out)):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name + "_gbs"] = src.numel() * src.element_size() / (e0.elapsed_time(e1) * 1e6)
+    out["transfer_ms_per_step"] = (host_in.numel() * 4 / (out["h2d_gbs"] * 1e6)
+                                   + host_out.numel() * 4 / (out["d2h_gbs"] * 1e6))
+    return out
+
+
 def graph_vs_stream(job, frames):
     """ms per frame of transform(0, frames) issued launch by launch and replayed as a captured
     CUDA graph (each after one untimed call); the job's graph option is restored."""
@@ -468,6 +487,7 @@ def run_gpu(args):
            "d2h_bytes_per_step": int((host_sqw.numel() + host_sq.numel()) * 4),
            "ms_per_step": ms_e2e,
            "host_memory": "pinned" if (pin_f and pin_w and pin_s) else "pageable (pinning refused)"}
+    e2e["host_link"] = host_link(frames, host_frames, sqw, host_sqw, stream)
 
     # per-stage kernel durations (CUDA events on the job's stream), one profiled pass
     job.profile(True)
