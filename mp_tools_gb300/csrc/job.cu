@@ -77,6 +77,7 @@ struct WeightArgs {
   float b_coh_f[MPSQ_MAX_SPECIES];
   float xff_f[MPSQ_MAX_SPECIES][9];
   float kappa_f, q0_f[3], qs_f[3][3], extra_f, wnorm_f;
+  float xb2_f[MPSQ_MAX_SPECIES][4];  // Cromer-Mann b_i log2(e): exp(-b_i s2) = 2^(-b_i log2(e) s2)
 };
 
 template <typename T>
@@ -153,6 +154,9 @@ struct mpsq_job {
   int* starts2 = nullptr;
   void* recs2 = nullptr;
   void* str2 = nullptr;
+  // per-atom preparation of the FP32 split path (counting pass -> scatter pass), per lane
+  void* prep = nullptr;
+  void* prep2 = nullptr;
   float2* b1_2 = nullptr;
   // one-phonon mode: displacement fields (n_species x 2 x n_row2 x n_row1, job precision)
   void* oneph_u = nullptr;
@@ -239,6 +243,7 @@ __device__ __forceinline__ bool prep_point(const float4* __restrict__ frame,
     if (p.use_range && at_ind) {
       const int4 ci = at_ind[j];
       const int c3[3] = {ci.x, ci.y, ci.z};
+#pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int c = c3[k] - p.n_row[k] / 2 - 1;
         if ((float)c < p.pos_min_f[k] || (float)c > p.pos_max_f[k]) return false;  // (:1109-1111)
@@ -246,6 +251,7 @@ __device__ __forceinline__ bool prep_point(const float4* __restrict__ frame,
     }
   } else {
     const float rr[3] = {r.x, r.y, r.z};
+#pragma unroll
     for (int k = 0; k < 3; ++k)  // (:1121-1128)
       if (!(rr[k] >= p.pos_min_f[k] - p.tol_f && rr[k] < p.pos_max_f[k] + p.tol_f)) return false;
   }
@@ -280,8 +286,11 @@ __device__ __forceinline__ bool prep_point(const float4* __restrict__ frame,
       if (p.window) {  // spatial Hann window (1+cos x)(1+cos y) (:1118)
         const int nw = p.dim == 2 ? 2 : 3;
         float f = 1.0f;
-        for (int k = 0; k < nw; ++k) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (k >= nw) break;
           float pr = 0.0f;
+#pragma unroll
           for (int b = 0; b < 3; ++b) pr = fmaf(p.axis_f[k][b], rf[b] - p.centre_f[b], pr);
           f *= 1.0f + cosf(pr * p.tpe_f[k]);
         }
@@ -395,6 +404,56 @@ __global__ void job_bin_kernel(const float4* __restrict__ frame, const int4* __r
                   cap, err);
 }
 
+// FP32 split path in two passes that prepare each atom once.  Pass 0 runs the selection, the
+// exact two-float cell split and the strength, keeps the result per atom (in locality order:
+// coalesced) and counts the atom's records per tile; pass 1 reads it back and writes the
+// records.  Per atom: int4 {s0 | s1 << 16, s2 | grid << 16 | comp << 24, d0, d1} (y = -1: not
+// transformed), d2, and the strength when strengths are not all 1.
+struct PrepCache {
+  int4* cell;
+  float* d2;
+  float2* c;   // null: unit strengths
+};
+
+__device__ __forceinline__ int low16_signed(int v) { return (v & 0xffff) - ((v & 0x8000) << 1); }
+
+__global__ void job_bin_count_split_kernel(const float4* __restrict__ frame,
+                                           const int4* __restrict__ at_ind,
+                                           const int* __restrict__ perm, PrepArgs p, SpreadArgs a,
+                                           int* cursor, PrepCache pc, int* err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n_atoms_frame) return;
+  const int64_t j = perm ? perm[i] : i;
+  PointPrep<float> q;
+  if (!prep_point<float>(frame, at_ind, p, a, j, q) || !q.split) {
+    pc.cell[i] = make_int4(0, -1, 0, 0);
+    return;
+  }
+  pc.cell[i] = make_int4((int)(((unsigned)q.sc[0] & 0xffffu) | ((unsigned)q.sc[1] << 16)),
+                         (int)(((unsigned)q.sc[2] & 0xffffu) | ((unsigned)q.grid << 16) |
+                               ((unsigned)q.comp << 24)),
+                         __float_as_int(q.dc[0]), __float_as_int(q.dc[1]));
+  pc.d2[i] = q.dc[2];
+  if (pc.c) pc.c[i] = make_float2(q.c.x, q.c.y);
+  emit_cells<float>(a, q.sc, q.dc, q.grid, q.comp, false, cursor, nullptr, nullptr, nullptr,
+                    make_float2(0.f, 0.f), nullptr, 0, 0, err);
+}
+
+__global__ void job_bin_scatter_split_kernel(int64_t n, PrepCache pc, SpreadArgs a, int* cursor,
+                                             const int* __restrict__ starts,
+                                             RecF* __restrict__ recs, float2* __restrict__ str,
+                                             int64_t cap, int* err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 r = __ldcs(pc.cell + i);
+  if (r.y == -1) return;
+  const int sc[3] = {low16_signed(r.x), r.x >> 16, low16_signed(r.y)};
+  const float dc[3] = {__int_as_float(r.z), __int_as_float(r.w), __ldcs(pc.d2 + i)};
+  const float2 c = pc.c ? __ldcs(pc.c + i) : make_float2(1.f, 0.f);
+  emit_cells<float>(a, sc, dc, (r.y >> 16) & 0xff, (r.y >> 24) & 0x7f, true, cursor, starts,
+                    recs, str, c, nullptr, 0, cap, err);
+}
+
 // Locality order of the atoms of one frame: a counting sort by the tile of each atom's first
 // support cell (atoms that are not transformed go to a last bucket, key nkeys).  Pass 0
 // counts, pass 1 writes perm[starts[key] + slot] = atom.
@@ -427,10 +486,28 @@ __global__ void job_perm_kernel(const float4* __restrict__ frame, const int4* __
   }
 }
 
+// 2^x on the special-function unit (PTX ex2.approx, relative error of order 2^-22; results
+// below the normal range flush to zero).
+__device__ __forceinline__ float ex2_sfu(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Species weight at s2 = kappa (|Q|^2 + extra) (mp_sqom56.f90:919-931): b_coh (neutron) or
+// the Cromer-Mann factor c + sum_i a_i exp(-b_i s2) (X-ray).  The FP32 path takes each
+// exponential as 2^(-(b_i log2 e) s2) on the SFU: one multiply and one SFU operation per term,
+// with an error below the FP32 rounding of s2 that feeds it.
 template <typename T>
 __device__ __forceinline__ T species_weight(const WeightArgs& w, int s, T s2) {
   if (w.weight_mode == MPSQ_WEIGHT_NEUTRON) return WP<T>::b(w, s);
   if (w.weight_mode == MPSQ_WEIGHT_XRAY) {
+    if constexpr (sizeof(T) == 4) {
+      float f = w.xff_f[s][8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) f = fmaf(w.xff_f[s][2 * i], ex2_sfu(-w.xb2_f[s][i] * s2), f);
+      return f;
+    }
     T f = WP<T>::x(w, s, 8);
     for (int i = 0; i < 4; ++i) f += WP<T>::x(w, s, 2 * i) * exp(-WP<T>::x(w, s, 2 * i + 1) * s2);
     return f;
@@ -1162,6 +1239,8 @@ static void job_free(mpsq_job* j) {
   job_release(j, j->starts2);
   job_release(j, j->recs2);
   job_release(j, j->str2);
+  job_release(j, j->prep);
+  job_release(j, j->prep2);
   job_release(j, j->b1_2);
   if (j->have_oneph_fft) cufftDestroy(j->oneph_fft);
   job_release(j, j->oneph_u);
@@ -1173,6 +1252,17 @@ static void job_free(mpsq_job* j) {
   for (auto& e : j->ev)
     if (e) cudaEventDestroy(e);
   delete j;
+}
+
+// Bytes of the per-atom preparation cache of the FP32 split path (0: not used): cell words
+// (16 B) and d2 (4 B) per atom, plus the strength (8 B, at offset 24 n) unless all are 1.
+static size_t prep_cache_bytes(int precision, int phase_rounding, bool unit_str, int64_t n) {
+  if (precision != MPSQ_FP32 || phase_rounding || n <= 0) return 0;
+  return (size_t)n * (unit_str ? 20 : 32);
+}
+static size_t prep_cache_bytes(const mpsq_job* j) {
+  return prep_cache_bytes(j->d.precision, j->pa.phase_rounding, !j->pa.has_qc && !j->pa.window,
+                          j->d.n_atoms_frame);
 }
 
 extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
@@ -1190,6 +1280,9 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
   b += d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision));
   b += (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8;
   b += d->n_atoms_frame * 4 + (int64_t)(std::max(1, ng) * g.n_tiles + 2) * 8;  // locality order
+  const int64_t prep = (int64_t)prep_cache_bytes(d->precision, d->phase_rounding, false,
+                                                 d->n_atoms_frame);  // per-atom preparation
+  b += prep;
   const int64_t store = d->q_slab > 0 ? g.m[0] * g.m[1] * std::min<int64_t>(d->q_slab, g.m[2])
                                       : g.n_modes;                      // modes per frame kept
   b += (int64_t)d->n_frames * store * (int64_t)csize(d->precision);     // cs(t,Q)
@@ -1201,7 +1294,7 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
     const int64_t b1 = (int64_t)std::max(1, ng) * g.nf[2] * g.nf[1] * (2 * (g.m[0] / 2) + 1) * 8;
     b += b1;
     b += (int64_t)std::max(1, ng) * g.n_fine * 8 + (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8 +
-         d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision)) + b1;
+         d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision)) + b1 + prep;
   } else {
     b += g.n_fine * (int64_t)csize(d->precision) / 4;  // cuFFT work area (estimate)
   }
@@ -1327,6 +1420,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   for (int s = 0; s < d->n_species; ++s) {
     w.b_coh_f[s] = (float)w.b_coh[s];
     for (int i = 0; i < 9; ++i) w.xff_f[s][i] = (float)w.xff[s][i];
+    for (int i = 0; i < 4; ++i) w.xb2_f[s][i] = (float)(w.xff[s][2 * i + 1] * M_LOG2E);
   }
   w.kappa_f = (float)w.kappa;
   for (int b = 0; b < 3; ++b) {
@@ -1361,6 +1455,8 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
   A((void**)&j->perm_starts, sizeof(int) * (nkeys + 2));
   A(&j->recs, (size_t)j->cap * rsize(prec));
   A(&j->str, (size_t)j->cap * cs);
+  const size_t prep_b = prep_cache_bytes(j);
+  if (prep_b) A(&j->prep, prep_b);
   j->slab_nz = d->q_slab > 0 ? std::min<int64_t>(d->q_slab, j->g.m[2]) : 0;
   const int64_t store = j->store_modes();
   A(&j->cs, (size_t)d->n_frames * store * cs);
@@ -1415,7 +1511,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
     const char* lanes = getenv("MPSQ_LANES");
     const size_t extra = (size_t)a.ngrid * j->g.n_fine * cs + 2 * sizeof(int) * (nkeys + 1) +
                          (size_t)j->cap * (rsize(prec) + cs) +
-                         sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0];
+                         sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0] + prep_b;
     size_t free_b = 0, total_b = 0;
     if (!d->stream_ordered && d->n_frames > 1 && !(lanes && strcmp(lanes, "1") == 0) &&
         cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && extra * 4 < free_b) {
@@ -1431,6 +1527,7 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
       A2(&j->recs2, (size_t)j->cap * rsize(prec));
       A2(&j->str2, (size_t)j->cap * cs);
       A2((void**)&j->b1_2, sizeof(float2) * (size_t)a.ngrid * n2 * n1 * j->K[0]);
+      if (prep_b) A2(&j->prep2, prep_b);
       if (e2 == cudaSuccess) {
         j->lane2 = true;
       } else {  // run with one lane
@@ -1441,7 +1538,8 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
         cudaFree(j->recs2);
         cudaFree(j->str2);
         cudaFree(j->b1_2);
-        j->fine2 = j->recs2 = j->str2 = nullptr;
+        cudaFree(j->prep2);
+        j->fine2 = j->recs2 = j->str2 = j->prep2 = nullptr;
         j->counts2 = j->starts2 = nullptr;
         j->b1_2 = nullptr;
       }
@@ -1547,20 +1645,38 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
     void* const fine = odd ? j->fine2 : j->fine;
     float2* const b1 = odd ? j->b1_2 : j->b1;
     const float4* frame = j->traj + (size_t)t * j->d.n_atoms_frame;
+    // FP32 split path: atoms prepared once, by the counting pass
+    const bool cached = sizeof(T) == 4 && j->prep != nullptr;
+    PrepCache pc{};
+    if (cached) {
+      char* base = static_cast<char*>(odd ? j->prep2 : j->prep);
+      const size_t n = (size_t)j->d.n_atoms_frame;
+      pc.cell = reinterpret_cast<int4*>(base);
+      pc.d2 = reinterpret_cast<float*>(base + 16 * n);
+      pc.c = unit_str ? nullptr : reinterpret_cast<float2*>(base + 24 * n);
+    }
     if (mark(0)) return MPSQ_ERR_CUDA;
     PhaseRange bin_range("mpsq:sort");
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, starts,
-                                                 (R*)recs, (C*)str, j->cap, j->err);
+      if (cached)
+        job_bin_count_split_kernel<<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, pc,
+                                                     j->err);
+      else
+        job_bin_kernel<T, false><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts,
+                                                   starts, (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
     int rc = launch_scan<T>(counts, starts, nkeys, s);
     if (rc) return rc;
     MPSQ_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), s));
     if (j->ngroups > 0) {
-      job_bin_kernel<T, true><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts, starts,
-                                                (R*)recs, (C*)str, j->cap, j->err);
+      if (cached)
+        job_bin_scatter_split_kernel<<<nb, bt, 0, s>>>(j->d.n_atoms_frame, pc, a, counts, starts,
+                                                       (RecF*)recs, (float2*)str, j->cap, j->err);
+      else
+        job_bin_kernel<T, true><<<nb, bt, 0, s>>>(frame, j->at_ind, perm, j->pa, a, counts,
+                                                  starts, (R*)recs, (C*)str, j->cap, j->err);
       MPSQ_LAUNCH_CHECK();
     }
     if (mark(1)) return MPSQ_ERR_CUDA;

@@ -348,8 +348,9 @@ class SqomJob:
         chunks of `chunk` frames (the first one `first_chunk` frames, to start computing
         early) on a second CUDA stream and transforms every chunk on the job's stream as soon
         as it has arrived, so the upload of chunk c+1 overlaps the transform of chunk c.
-        Uploads start after all work already queued on the job's stream, which may still read
-        the previous trajectory."""
+        The first call's uploads start after all work already queued on the job's stream;
+        a later call with the same chunking uploads each chunk as soon as the previous call has
+        transformed that chunk, so it overlaps the previous call's remaining work."""
         import torch
         if hasattr(frames, "is_cuda"):
             if frames.is_cuda:
@@ -369,21 +370,38 @@ class SqomJob:
         if self._copy_stream is None:
             self._copy_stream = torch.cuda.Stream()
         cs = self._copy_stream
-        tail = torch.cuda.Event()
-        tail.record(job_stream)
-        cs.wait_event(tail)
         frame_bytes = self.n_atoms_frame * 16
         bounds = [0] + list(range(min(max(1, first_chunk), F), F, chunk)) + [F]
-        for c0, c1 in zip(bounds[:-1], bounds[1:]):
+        # A chunk's frames may be overwritten once the previous call has transformed them (the
+        # transform reads positions only while binning; the maps read the amplitude store), so
+        # with the same chunking each upload waits for that chunk's transform of the previous
+        # call instead of for everything queued on the job's stream: the next call's uploads
+        # run while this call still computes.
+        prev = self._chunk_done if getattr(self, "_chunk_bounds", None) == bounds else None
+        if prev is None:
+            tail = torch.cuda.Event()
+            tail.record(job_stream)
+            cs.wait_event(tail)
+        done = []
+        for i, (c0, c1) in enumerate(zip(bounds[:-1], bounds[1:])):
             n = c1 - c0
+            if prev is not None:
+                cs.wait_event(prev[i])
             check(L.mpsq_job_set_frames_on(self._h, C.c_void_p(base + c0 * frame_bytes), c0, n, 1,
                                            C.c_void_p(cs.cuda_stream)), "set_frames_on")
             ev = torch.cuda.Event()
             ev.record(cs)
             job_stream.wait_event(ev)
             self.transform(c0, n)
+            consumed = torch.cuda.Event()
+            consumed.record(job_stream)
+            done.append(consumed)
+        self._chunk_bounds, self._chunk_done = bounds, done
         # copies of earlier outputs to the host go after the uploads, on the same stream
         self._flush_outputs(cs)
+        # host memory stays alive until its copies are ordered: this call's and, as the next
+        # call's uploads no longer wait for the whole stream, the previous call's
+        self._keep_prev = getattr(self, "_keep", None)
         self._keep = frames
 
     def transform(self, first: int = 0, count: int | None = None):
