@@ -126,6 +126,26 @@ __device__ __forceinline__ float clear_low13(float v) {
   return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
 }
 
+// Two FP32 lanes per instruction (PTX mul/sub .f32x2, IEEE round-to-nearest per lane).
+__device__ __forceinline__ float2 mul_f32x2(float2 a, float2 b) {
+  unsigned long long pa, pb, r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pa), "l"(pb));
+  float2 o;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(r));
+  return o;
+}
+__device__ __forceinline__ float2 sub_f32x2(float2 a, float2 b) {
+  unsigned long long pa, pb, r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pa), "l"(pb));
+  float2 o;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(r));
+  return o;
+}
+
 __device__ __forceinline__ uint32_t pack_f16x2(float first, float second) {
   const __half2 h = __floats2half2_rn(first, second);   // first -> low 16 bits
   uint32_t u;
@@ -158,13 +178,15 @@ __device__ __forceinline__ void build_a(const MmaSmem<W>& sm, int p, int first, 
                                         uint32_t (&ah)[4], uint32_t (&al)[4]) {
   const float2 zA = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t]);
   const float2 zB = *reinterpret_cast<const float2*>(&sm.kz[p][first + 2 * t + 8]);
-  const float a[8] = {yA0.x * zA.x, yA0.y * zA.y, yA1.x * zA.x, yA1.y * zA.y,
-                      yB0.x * zB.x, yB0.y * zB.y, yB1.x * zB.x, yB1.y * zB.y};
+  // products and lo terms two lanes per instruction
+  const float2 a[4] = {mul_f32x2(yA0, zA), mul_f32x2(yA1, zA), mul_f32x2(yB0, zB),
+                       mul_f32x2(yB1, zB)};
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const float h0 = clear_low13(a[2 * j]), h1 = clear_low13(a[2 * j + 1]);
-    ah[j] = pack_f16x2(h0, h1);
-    al[j] = pack_f16x2(a[2 * j] - h0, a[2 * j + 1] - h1);
+    const float2 h = make_float2(clear_low13(a[j].x), clear_low13(a[j].y));
+    ah[j] = pack_f16x2(h.x, h.y);
+    const float2 l = sub_f32x2(a[j], h);
+    al[j] = pack_f16x2(l.x, l.y);
   }
 }
 
