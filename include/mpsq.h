@@ -306,22 +306,36 @@ int mpsq_job_set_q_slab(mpsq_job* job, int64_t z0);
  *   MPSQ_OPT_SPREAD 0 (default): tensor-core spreading of packed real species pairs;
  *                   1: the CUDA-core FP32 spreading kernel.
  *   MPSQ_OPT_XROWS  rows per CTA of the pruned X pass, 4 or 8 (default).
- *   MPSQ_OPT_LANES  frame lanes used when the job has a second one, 1 or 2 (default). */
+ *   MPSQ_OPT_LANES  frame lanes used when the job has a second one, 1 or 2 (default).
+ *   MPSQ_OPT_ZSLAB  0 (default): spreading, then passes X and Y over whole fine grids;
+ *                   a multiple of 16: spreading and passes X and Y run slab by slab of that
+ *                   many fine-grid planes over one slab-sized region, which stays in L2
+ *                   (FP32 volumes on the pruned transform with tensor-core pair spreading;
+ *                   ignored otherwise).
+ *   MPSQ_OPT_REPRODUCIBLE  0 (default): records are accumulated within a tile in the order
+ *                   the binning's atomics left them, so repeated runs agree to FP32 rounding;
+ *                   1: the tensor-core spreading orders each tile's records by content first,
+ *                   so that every run, schedule (graph, lanes, z-slabs, other jobs on the GPU)
+ *                   and job instance gives bit-identical results (FP32 volumes with packed
+ *                   pairs; about 20 % more spreading time). */
 #define MPSQ_OPT_GRAPH   1
 #define MPSQ_OPT_SPREAD  2
 #define MPSQ_OPT_XROWS   3
 #define MPSQ_OPT_LANES   4
+#define MPSQ_OPT_ZSLAB   5
+#define MPSQ_OPT_REPRODUCIBLE 6
 int mpsq_job_set_option(mpsq_job* job, int option, int value);
 int mpsq_job_get_option(const mpsq_job* job, int option, int* value);
 
 /* Autotuner (no reference counterpart): times mpsq_job_transform(job, first, count) under
  * every combination of the choices above that applies to the job (graph replay, spreading
- * kernel, X-pass rows, frame lanes; three calls each, the first untimed), keeps the fastest
- * and sets it on the job.  With a cache_path, a choice recorded there for the same job shape
- * (precision, fine grid, width, grids, packing, pruned transform, lanes) and SM count is taken
- * without timing, and a new choice is appended.  choice[4] (optional) returns
- * {graph, spread, xrows, lanes}; best_ms (optional) the time of one call.  The timed calls
- * rewrite the amplitudes of the same frames. */
+ * kernel, X-pass rows, frame lanes, z-slab pipeline at 64 planes or none; three calls each,
+ * the first untimed), keeps the fastest and sets it on the job.  With a cache_path, a choice
+ * recorded there for the same job shape (precision, fine grid, width, grids, packing, pruned
+ * transform, lanes) and SM count is taken without timing, and a new choice is appended.
+ * choice[4] (optional) returns {graph, spread, xrows, lanes} (the z-slab choice:
+ * mpsq_job_get_option); best_ms (optional) the time of one call.  The timed calls rewrite the
+ * amplitudes of the same frames. */
 int mpsq_job_autotune(mpsq_job* job, int32_t first, int32_t count, const char* cache_path,
                       int* choice, double* best_ms);
 

@@ -15,7 +15,7 @@ FP32, FP64 = 0, 1
 CELL, BULK = 0, 1
 WEIGHT_UNIT, WEIGHT_NEUTRON, WEIGHT_XRAY = 1, 2, 3
 FF_MP_SQOM, FF_STANDARD = 0, 1
-OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES = 1, 2, 3, 4
+OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES, OPT_ZSLAB, OPT_REPRODUCIBLE = 1, 2, 3, 4, 5, 6
 
 ERR_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_ALLOC", 3: "ERR_CUDA", 4: "ERR_CUFFT",
              5: "ERR_STATE", 6: "ERR_DEVICE"}

@@ -342,15 +342,21 @@ int launch_scan(const int* counts, int* starts, int64_t n, cudaStream_t s);
 template <typename T>
 int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,
-                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core = true);
+                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core = true,
+                  bool repro = false);
 
 // Tensor-core spreading of packed real species pairs (3D, 16^3 tiles, FP32 grid); strengths
 // must be real with |s| <= 8.  Selected by default; MPSQ_SPREAD=fma in the environment keeps
 // the CUDA-core kernel instead.
 bool spread_pair_mma_enabled();
+// Keys [key0, key0 + nkeys); a z-slab launch (gstride > 0) writes the tiles' cells at plane
+// z - z0 of grids gstride elements apart (otherwise the full grids, n_fine apart).  repro:
+// each tile's records are ordered by content before they are accumulated, so that the result
+// does not depend on the order they were binned in.
 int launch_spread_pair_mma(const SpreadArgs& a, const RecF* recs, const int* idx,
                            const float2* cv, int64_t c_stride, const int* starts, int nkeys,
-                           int ntrans, float2* fine, cudaStream_t s);
+                           int ntrans, float2* fine, cudaStream_t s, int64_t key0 = 0,
+                           int z0 = 0, int64_t gstride = 0, bool repro = false);
 
 // cuFFT plan cache key
 int make_fft_plan(const GridGeom& g, int ngrid, int precision, cudaStream_t s, cufftHandle* h);

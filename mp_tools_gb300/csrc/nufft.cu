@@ -644,11 +644,12 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
                               const int* idx, const typename Cplx<T>::type* cv, int64_t c_stride,
                               const int* starts, int nkeys, int ntrans, bool real_pair,
                               typename Cplx<T>::type* fine, cudaStream_t s,
-                              bool tensor_core = true) {
+                              bool tensor_core = true, bool repro = false) {
   if constexpr (std::is_same<T, float>::value && DIM == 3) {
     if (a.tile[0] == 16 && a.tile[1] == 16 && a.tile[2] == 16 && a.w >= 3 && a.w <= 8) {
       if (real_pair && tensor_core && spread_pair_mma_enabled())
-        return launch_spread_pair_mma(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+        return launch_spread_pair_mma(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s,
+                                      0, 0, 0, repro);
       dim3 grid((unsigned)nkeys, (unsigned)ntrans);
       const int rp = real_pair ? 1 : 0;
       switch (a.w) {
@@ -703,19 +704,19 @@ static int launch_spread_impl(const SpreadArgs& a, const typename RecOf<T>::type
 template <typename T>
 int launch_spread(const SpreadArgs& a, const typename RecOf<T>::type* recs,
                   const typename Cplx<T>::type* str, const int* starts, bool real_pair,
-                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core) {
+                  typename Cplx<T>::type* fine, cudaStream_t s, bool tensor_core, bool repro) {
   constexpr int NT = sizeof(T) == 4 ? 256 : 128;
   int nkeys = (int)(a.n_tiles * a.ngrid);
   if (a.dim == 3)
     return launch_spread_impl<T, 3, NT>(a, recs, nullptr, str, 0, starts, nkeys, 1, real_pair,
-                                        fine, s, tensor_core);
+                                        fine, s, tensor_core, repro);
   return launch_spread_impl<T, 2, NT>(a, recs, nullptr, str, 0, starts, nkeys, 1, real_pair,
-                                      fine, s, tensor_core);
+                                      fine, s, tensor_core, repro);
 }
 template int launch_spread<float>(const SpreadArgs&, const RecF*, const float2*, const int*, bool,
-                                  float2*, cudaStream_t, bool);
+                                  float2*, cudaStream_t, bool, bool);
 template int launch_spread<double>(const SpreadArgs&, const RecD*, const double2*, const int*,
-                                   bool, double2*, cudaStream_t, bool);
+                                   bool, double2*, cudaStream_t, bool, bool);
 
 int make_fft_plan(const GridGeom& g, int ngrid, int precision, cudaStream_t s, cufftHandle* h) {
   long long n[3];

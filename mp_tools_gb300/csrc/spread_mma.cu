@@ -57,9 +57,11 @@ struct MmaSmem {
   int lz[kCh];                           // start z of the record in each slot
   RecF rec[kCh];                         // the record sorted into each slot
   float str[kCh];                        // its real strength
+  int member[kCh];                       // the chunk's records grouped by key (chunk order)
   int count[2 * kKeys];
   int base[2 * kKeys];
-  int n0, b1, n1;
+  int tcount[2 * kKeys];                 // records per key over the whole tile (large tiles)
+  int n0, b1, n1, msel;
 };
 
 // The ES kernel value of cell i of a support, phi(z) = exp(beta (sqrt(1 - z^2) - 1)) at
@@ -260,19 +262,20 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
   }
 }
 
-template <int W>
+template <int W, bool REPRO>
 __global__ void __launch_bounds__(256, 3)
     spread3_pair_mma_kernel(SpreadArgs a, const RecF* __restrict__ recs,
                             const int* __restrict__ idx, const float2* __restrict__ cv,
                             int64_t c_stride, const int* __restrict__ starts,
-                            float2* __restrict__ fine, const EsPoly<W> poly) {
+                            float2* __restrict__ fine, const EsPoly<W> poly, int64_t key0,
+                            int z0, int64_t gstride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MmaSmem<W>& sm = *reinterpret_cast<MmaSmem<W>*>(smem_raw);
   constexpr int K1 = MmaSmem<W>::kKeys;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int p0 = 2 * warp;
-  const int64_t key = blockIdx.x;
+  const int64_t key = key0 + blockIdx.x;
   const int trans = blockIdx.y;
   const int keygrid = (int)(key / a.n_tiles);
   const int tile = (int)(key - (int64_t)keygrid * a.n_tiles);
@@ -287,30 +290,82 @@ __global__ void __launch_bounds__(256, 3)
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc_re[i][j][k] = acc_im[i][j][k] = 0.0f;
   const int r0 = starts[key], r1 = starts[key + 1];
-  for (int c0 = r0; c0 < r1; c0 += kCap) {
-    const int n = min(kCap, r1 - c0);
+  // Chunks of at most kCap records, in binning order.  Reproducible order (REPRO): all of the
+  // tile's records when they fit one chunk; otherwise whole (component, start z) keys, counted
+  // first, packed greedily into chunks (keys in order), so that the partition, like the order
+  // inside a chunk, does not depend on the order the records were binned in.  A single key
+  // with more than kCap records (an extremely dense tile) takes the binning order.
+  auto key_of = [&](const RecF& q) {
+    const int lz = ((q.packed >> 16) & 0xff) - 64;
+    return ((q.packed >> 24) & 1) * K1 + min(max(lz + W - 1, 0), K1 - 1);
+  };
+  auto strength = [&](int r) {
+    return !cv ? 1.0f : (idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r]).x;
+  };
+  bool by_key = false;
+  if (REPRO && r1 - r0 > kCap) {
+    for (int e = tid; e < 2 * K1; e += 256) sm.tcount[e] = 0;
+    __syncthreads();
+    for (int r = r0 + tid; r < r1; r += 256) atomicAdd(&sm.tcount[key_of(recs[r])], 1);
+    __syncthreads();
+    by_key = true;
+    for (int e = 0; e < 2 * K1; ++e) by_key = by_key && sm.tcount[e] <= kCap;
+  }
+  int c0 = r0, kb = 0;
+  for (;;) {
+    int n = 0, kb_hi = kb;
+    if (by_key) {
+      if (kb >= 2 * K1) break;
+      while (kb_hi < 2 * K1 && n + sm.tcount[kb_hi] <= kCap) n += sm.tcount[kb_hi++];
+    } else {
+      if (c0 >= r1) break;
+      n = min(kCap, r1 - c0);
+    }
     {  // zero the staging arrays (alignment-gap slots and out-of-support rows must read 0)
       uint4* z4 = reinterpret_cast<uint4*>(&sm.ky[0][0]);
       constexpr int nz = (int)((sizeof(sm.ky) + sizeof(sm.kz) + sizeof(sm.kxh) + sizeof(sm.kxl)) / 16);
       for (int e = tid; e < nz; e += 256) z4[e] = make_uint4(0u, 0u, 0u, 0u);
       for (int e = tid; e < 2 * K1; e += 256) sm.count[e] = 0;
+      if (tid == 0) sm.msel = 0;
     }
     __syncthreads();
-    // 1. rank every record within its (component, start z) key
+    // 1. the chunk's records into slots 0..n-1 in any order (by position, or selected by key)
     RecF rec;
     float sv = 0.0f;
     int k = 0, rank = 0;
+    if (!REPRO) {
+      if (tid < n) {
+        rec = recs[c0 + tid];
+        sv = strength(c0 + tid);
+      }
+    } else if (!by_key) {
+      if (tid < n) {
+        sm.rec[tid] = recs[c0 + tid];
+        sm.str[tid] = strength(c0 + tid);
+      }
+    } else {
+      for (int r = r0 + tid; r < r1; r += 256) {
+        const RecF q = recs[r];
+        const int k = key_of(q);
+        if (k >= kb && k < kb_hi) {
+          const int at = atomicAdd(&sm.msel, 1);
+          sm.rec[at] = q;
+          sm.str[at] = strength(r);
+        }
+      }
+    }
+    if (REPRO) __syncthreads();
+    // 2. group the records by key (component, start z)
     if (tid < n) {
-      const int r = c0 + tid;
-      rec = recs[r];
-      sv = !cv ? 1.0f : (idx ? cv[(int64_t)trans * c_stride + idx[r]] : cv[r]).x;
-      const int lz = ((rec.packed >> 16) & 0xff) - 64;
-      const int comp = (rec.packed >> 24) & 1;
-      k = comp * K1 + min(max(lz + W - 1, 0), K1 - 1);
+      if (REPRO) {
+        rec = sm.rec[tid];
+        sv = sm.str[tid];
+      }
+      k = key_of(rec);
       rank = atomicAdd(&sm.count[k], 1);
     }
     __syncthreads();
-    // 2. exclusive scan of the key counts (one warp; K1 <= 23 keys per component); the
+    // 3. exclusive scan of the key counts (one warp; K1 <= 23 keys per component); the
     //    second component starts on a multiple of 16
     if (warp == 0) {
       const int c0n = lane < K1 ? sm.count[lane] : 0;
@@ -337,14 +392,40 @@ __global__ void __launch_bounds__(256, 3)
       }
     }
     __syncthreads();
-    // 3. place each record in its sorted slot
+    // 4. the slot within the key: the binning order, or (REPRO) the order by content (cell
+    //    offsets, then offsets and strength bits), so that the slots, and with them the
+    //    accumulation order, follow from the record set alone; records equal in every bit may
+    //    take either order
+    int pos = rank;
+    if (REPRO) {
+      if (tid < n) sm.member[sm.base[k] + rank] = tid;
+      __syncthreads();
+    }
+    if (REPRO && tid < n) {
+      pos = 0;
+      const uint64_t mine = ((uint64_t)(uint32_t)rec.packed << 32) | __float_as_uint(rec.dz);
+      const int b = sm.base[k], cnt = sm.count[k];
+      for (int q = b; q < b + cnt; ++q) {
+        const int o = sm.member[q];
+        const RecF& u = sm.rec[o];
+        const uint64_t other = ((uint64_t)(uint32_t)u.packed << 32) | __float_as_uint(u.dz);
+        bool before = other < mine;
+        if (other == mine && o != tid) {
+          const uint32_t a[3] = {__float_as_uint(u.dy), __float_as_uint(u.dx), __float_as_uint(sm.str[o])};
+          const uint32_t m[3] = {__float_as_uint(rec.dy), __float_as_uint(rec.dx), __float_as_uint(sv)};
+          before = a[0] != m[0] ? a[0] < m[0] : a[1] != m[1] ? a[1] < m[1] : a[2] != m[2] ? a[2] < m[2] : o < tid;
+        }
+        pos += before ? 1 : 0;
+      }
+    }
+    if (REPRO) __syncthreads();
     if (tid < n) {
-      const int slot = sm.base[k] + rank;
+      const int slot = sm.base[k] + pos;
       sm.rec[slot] = rec;
       sm.str[slot] = sv;
     }
     __syncthreads();
-    // 4. thread t evaluates the kernel of the record in slot t and writes its support rows
+    // 5. thread t evaluates the kernel of the record in slot t and writes its support rows
     //    (consecutive threads write consecutive columns of a row: no bank conflicts)
     {
       const int st = tid;
@@ -380,14 +461,16 @@ __global__ void __launch_bounds__(256, 3)
     const int n0 = sm.n0, b1 = sm.b1, n1 = sm.n1;
     mma_region<W>(sm, 0, (n0 + 15) >> 4, n0, p0, g, t, acc_re);
     mma_region<W>(sm, b1 >> 4, (b1 + n1 + 15) >> 4, b1 + n1, p0, g, t, acc_im);
-    if (c0 + kCap < r1) __syncthreads();   // another chunk reuses the staging arrays
+    c0 += kCap;
+    kb = kb_hi;
+    __syncthreads();   // another chunk reuses the staging arrays
   }
-  float2* out = fine + (int64_t)(keygrid + trans) * a.n_fine;
+  float2* out = fine + (int64_t)(keygrid + trans) * gstride;
   const int64_t nf0 = a.nf[0], nf1 = a.nf[1];
   const float sc = 1.0f / 1048576.0f;
 #pragma unroll
   for (int pi = 0; pi < 2; ++pi) {
-    const int64_t zrow = ((int64_t)tz * 16 + p0 + pi) * nf1 + (int64_t)ty * 16;
+    const int64_t zrow = ((int64_t)tz * 16 - z0 + p0 + pi) * nf1 + (int64_t)ty * 16;
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt) {
       const int64_t xcol = (int64_t)tx * 16 + nt * 8 + 2 * t;
@@ -405,13 +488,17 @@ __global__ void __launch_bounds__(256, 3)
 template <int W>
 int launch_w(const SpreadArgs& a, const RecF* recs, const int* idx, const float2* cv,
              int64_t c_stride, const int* starts, int nkeys, int ntrans, float2* fine,
-             cudaStream_t s) {
+             cudaStream_t s, int64_t key0, int z0, int64_t gstride, bool repro) {
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(spread3_pair_mma_kernel<W>,
+    attr = cudaFuncSetAttribute(spread3_pair_mma_kernel<W, false>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(MmaSmem<W>));
+    if (attr == cudaSuccess)
+      attr = cudaFuncSetAttribute(spread3_pair_mma_kernel<W, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(MmaSmem<W>));
   });
   if (attr != cudaSuccess) return fail(MPSQ_ERR_CUDA, "spread mma attribute: %s", cudaGetErrorString(attr));
   static std::mutex mu;
@@ -426,8 +513,13 @@ int launch_w(const SpreadArgs& a, const RecF* recs, const int* idx, const float2
     }
     p = poly;
   }
-  spread3_pair_mma_kernel<W><<<dim3((unsigned)nkeys, (unsigned)ntrans), 256, sizeof(MmaSmem<W>), s>>>(
-      a, recs, idx, cv, c_stride, starts, fine, p);
+  const dim3 grid((unsigned)nkeys, (unsigned)ntrans);
+  if (repro)
+    spread3_pair_mma_kernel<W, true><<<grid, 256, sizeof(MmaSmem<W>), s>>>(
+        a, recs, idx, cv, c_stride, starts, fine, p, key0, z0, gstride);
+  else
+    spread3_pair_mma_kernel<W, false><<<grid, 256, sizeof(MmaSmem<W>), s>>>(
+        a, recs, idx, cv, c_stride, starts, fine, p, key0, z0, gstride);
   MPSQ_LAUNCH_CHECK();
   return MPSQ_OK;
 }
@@ -444,18 +536,29 @@ bool spread_pair_mma_enabled() {
 
 int launch_spread_pair_mma(const SpreadArgs& a, const RecF* recs, const int* idx,
                            const float2* cv, int64_t c_stride, const int* starts, int nkeys,
-                           int ntrans, float2* fine, cudaStream_t s) {
+                           int ntrans, float2* fine, cudaStream_t s, int64_t key0, int z0,
+                           int64_t gstride, bool repro) {
   if (a.dim != 3 || a.tile[0] != 16 || a.tile[1] != 16 || a.tile[2] != 16)
     return fail(MPSQ_ERR_ARG, "spread mma: 16^3 tiles only");
   if ((reinterpret_cast<uintptr_t>(fine) & 15) != 0 || (a.nf[0] & 1) != 0)
     return fail(MPSQ_ERR_ARG, "spread mma: grid must be 16-byte aligned with even rows");
+  if (gstride <= 0) {
+    key0 = 0;
+    z0 = 0;
+    gstride = a.n_fine;
+  }
+  if (nkeys <= 0) return MPSQ_OK;
+#define MPSQ_W(W) \
+  launch_w<W>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s, key0, z0, gstride, \
+              repro)
   switch (a.w) {
-    case 3: return launch_w<3>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
-    case 4: return launch_w<4>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
-    case 5: return launch_w<5>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
-    case 6: return launch_w<6>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
-    case 7: return launch_w<7>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
-    case 8: return launch_w<8>(a, recs, idx, cv, c_stride, starts, nkeys, ntrans, fine, s);
+    case 3: return MPSQ_W(3);
+    case 4: return MPSQ_W(4);
+    case 5: return MPSQ_W(5);
+    case 6: return MPSQ_W(6);
+    case 7: return MPSQ_W(7);
+    case 8: return MPSQ_W(8);
+#undef MPSQ_W
     default: return fail(MPSQ_ERR_ARG, "spread mma: kernel width %d not compiled", a.w);
   }
 }

@@ -87,10 +87,13 @@ class FrameSource:
 class GpuExecutor:
     """Runs a request as a stream-ordered SqomJob on its own stream.  A request whose whole
     amplitude store would not fit in the budget runs slab by slab along kz (q_slab: the largest
-    slab that fits), recomputing the transform of every frame per slab."""
+    slab that fits), recomputing the transform of every frame per slab.  Jobs run with the
+    reproducible in-tile order (a request's results do not depend on what else shares the GPU)
+    unless `reproducible` is set False."""
 
     budget = None                  # set by the server: the device memory admissions share
     pin_limit = 256 << 20          # map bytes up to which results go to pinned host buffers
+    reproducible = True
 
     def _describe(self, req, q_slab):
         return SqomJob.describe(req.grid, species_counts=req.counts, n_frames=req.n_frames,
@@ -141,6 +144,7 @@ class GpuExecutor:
         job = SqomJob(req.grid, species_counts=req.counts, n_frames=req.n_frames,
                       n_atoms_frame=req.n_atoms, stream=stream.cuda_stream,
                       stream_ordered=True, q_slab=q_slab, **req.job_kwargs)
+        job.set_option(_lib.OPT_REPRODUCIBLE, int(self.reproducible))
         nq = req.grid.n_modes
         F = req.n_frames
         n_bins = self._n_bins(req)

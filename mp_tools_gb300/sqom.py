@@ -436,7 +436,8 @@ class SqomJob:
         return self.info()["n_grids"]
 
     def set_option(self, option: int, value: int):
-        """Run-time choice (_lib.OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES); see mpsq.h."""
+        """Run-time choice (_lib.OPT_GRAPH, OPT_SPREAD, OPT_XROWS, OPT_LANES, OPT_ZSLAB); see
+        mpsq.h."""
         check(_lib.load().mpsq_job_set_option(self._h, int(option), int(value)), "set_option")
 
     def get_option(self, option: int) -> int:
@@ -455,7 +456,8 @@ class SqomJob:
                                             cache.encode() if cache else None, ch, C.byref(ms)),
               "autotune")
         return {"graph": ch[0], "spread": ("tensor-core", "cuda-core")[ch[1]], "xrows": ch[2],
-                "lanes": ch[3], "ms_per_call": ms.value, "frames_per_call": count}
+                "lanes": ch[3], "zslab": self.get_option(_lib.OPT_ZSLAB),
+                "ms_per_call": ms.value, "frames_per_call": count}
 
     @property
     def slab_planes(self) -> int:

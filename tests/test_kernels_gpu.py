@@ -134,9 +134,8 @@ def test_tensor_core_spread_against_direct_sum(cuda, eps, tol):
 
 def test_transform_from_host_equals_device_upload(cuda):
     """Chunked upload on a second stream (pinned host tensor) gives the amplitudes of one upload
-    followed by the transform, also when the job is run twice back to back.  (Equal up to FP32
-    rounding: the order of records within a tile, and so of the sums, follows the binning's
-    atomics and is not fixed from run to run.)"""
+    followed by the transform, bit for bit with the reproducible order, also when the job is
+    run twice back to back."""
     import torch
     fr, counts = _alloy(n_atoms=3000, F=40)
     grid = sql.SqlGrid(4.0, (30.0,) * 3)
@@ -145,6 +144,8 @@ def test_transform_from_host_equals_device_upload(cuda):
     a = SqomJob(grid, **kw)
     b = SqomJob(grid, **kw)
     try:
+        for job in (a, b):
+            job.set_option(_lib.OPT_REPRODUCIBLE, 1)
         a.set_frames(fr)
         a.transform()
         a.sync()
@@ -152,7 +153,7 @@ def test_transform_from_host_equals_device_upload(cuda):
         for _ in range(2):
             b.transform_from_host(pinned, chunk=7)
         b.sync()
-        assert rel_l2(b.amplitudes(), a.amplitudes()) < 1e-6
+        assert np.array_equal(b.amplitudes(), a.amplitudes())
     finally:
         a.close()
         b.close()
@@ -168,6 +169,7 @@ fr, counts = T._alloy(n_atoms=4000, F=9)
 grid = sql.SqlGrid(4.0, (30.0,) * 3)
 job = T.SqomJob(grid, species_counts=counts, n_frames=fr.shape[0], precision=_lib.FP32, eps=1e-6,
                 n_atoms_frame=fr.shape[1], weight_mode=_lib.WEIGHT_XRAY, xff=[T.XFF_AL, T.XFF_U])
+job.set_option(_lib.OPT_REPRODUCIBLE, 1)
 job.set_frames(fr)
 job.transform(0, 4)            # even count
 job.transform(4, 5)            # odd count, second call
@@ -181,7 +183,8 @@ XFF_U = [36.0228, 0.5293, 23.4128, 3.3253, 14.9491, 16.0927, 4.1880, 100.6130, 1
 
 def test_two_frame_lanes_match_one_lane(cuda, tmp_path):
     """Frames alternating between the job's stream and the second lane give the results of a
-    single lane (MPSQ_LANES=1, child process) to FP32 rounding, over two transform calls."""
+    single lane (MPSQ_LANES=1, child process) bit for bit (reproducible order), over two
+    transform calls."""
     out = {}
     for lanes in ("2", "1"):
         env = dict(os.environ)
@@ -193,7 +196,7 @@ def test_two_frame_lanes_match_one_lane(cuda, tmp_path):
         subprocess.run([sys.executable, "-c", _CHILD_LANES, str(ROOT), str(path)], check=True,
                        env=env, timeout=600)
         out[lanes] = np.load(path)
-    assert rel_l2(out["2"], out["1"]) < 2e-6
+    assert np.array_equal(out["2"], out["1"])
 
 
 def test_outputs_to_host_tensors_are_copied_asynchronously(cuda):
