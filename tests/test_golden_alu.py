@@ -147,3 +147,50 @@ def test_gpu_job_reproduces_reference_tables(cuda, precision):
                                    eps=1e-6 if precision == "fp32" else 1e-9)
     _compare(s, hist, 10.0, _product_post(s), tol=5e-6 if precision == "fp32" else 2e-6)
     _compare(s, hist, Q_RANGE_FULL, _product_post(s), tol=3e-4, q_min=10.0)
+
+
+@pytest.mark.gpu
+def test_gpu_high_q_band_is_the_tables_own_deviation(cuda):
+    """Bounds the 3e-4 band above 10 A^-1 from our side: the FP64 job's amplitudes at 3,000
+    random modes with 10 < |Q| <= 20 A^-1 equal the FP64 direct sum over all 30,000 atoms to
+    1e-8 (relative l2), and the FP32 job's |Q| histogram equals the FP64 job's in every bin
+    above 10 A^-1 to 2e-6 of the bin values' maximum, so this path's histogram there is exact to
+    far below the printed tables' deviation."""
+    from helpers import rel_l2
+    from mp_tools_gb300 import _lib, sql
+    from mp_tools_gb300.sqom import SqomJob
+    import oracle
+    s = _setup()
+    grid = sql.SqlGrid(Q_RANGE_FULL, (s["box"],) * 3)
+    n = grid.n_q[0]
+    frames = np.asarray(s["frame"].at_pos[None, :, :], np.float32)
+    n_hist = 1 + int(np.float32(grid.q_range) / np.float32(s["q_step"]))
+    job = SqomJob(grid, species_counts=s["counts"], n_frames=1, precision=_lib.FP64, eps=1e-9,
+                  store_species=True, n_atoms_frame=frames.shape[1])
+    try:
+        job.set_frames(frames)
+        job.transform()
+        job.sync()
+        h64 = job.radial_hist(grid.a_cell_inv, grid.d_q, s["q_step"], grid.q_range, n_hist,
+                              amp_scale=1.0 / float(sum(s["counts"])))
+        rng = np.random.default_rng(20)
+        k = rng.integers(-(n // 2), n // 2 + 1, size=(40000, 3))
+        q = np.linalg.norm(k * grid.d_q.astype(np.float64), axis=1)
+        k = k[(q > 10.0) & (q <= Q_RANGE_FULL)][:3000]
+        assert len(k) == 3000
+        flat = ((k[:, 2] + n // 2) * n + (k[:, 1] + n // 2)) * n + (k[:, 0] + n // 2)
+        got = job.amplitudes_at(flat)[0]
+    finally:
+        job.close()
+    r = frames[0, :, :3].astype(np.float64)
+    d = grid.d_q.astype(np.float64)
+    want = oracle.dirft_modes_tab(r[:, 0] * d[0], r[:, 1] * d[1], r[:, 2] * d[2],
+                                  np.ones(len(r)), -1, k)
+    assert rel_l2(got, want) < 1e-8
+    h32 = sql.transform_histogram(frames, s["counts"], grid, s["q_step"], precision=_lib.FP32,
+                                  eps=1e-6)
+    hi = int(10.0 / s["q_step"])
+    for a in range(h64.shape[0]):
+        for b in range(h64.shape[1]):
+            ref = h64[a, b, hi:]
+            assert np.max(np.abs(h32[a, b, hi:] - ref)) <= 2e-6 * np.max(np.abs(ref)), (a, b)
