@@ -135,6 +135,10 @@ struct mpsq_job {
   void* cs_species = nullptr;
   cufftHandle fft = 0;
   bool have_fft = false;
+  // volumes on cuFFT: x transforms over every row, then (z, y) transforms of the kept x columns
+  cufftHandle xfft[3] = {0, 0, 0};   // x rows; (z, y) of columns [0, h0]; of [n0 - h0, n0)
+  int xfft_h0 = 0;
+  bool have_xfft = false;
   int* err = nullptr;
   bool profile = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -1225,6 +1229,9 @@ static int job_layout(const mpsq_job_desc* d, EsKernel* es, GridGeom* g, int* ng
 static void job_free(mpsq_job* j) {
   if (!j) return;
   if (j->have_fft) cufftDestroy(j->fft);
+  if (j->have_xfft)
+    for (auto h : j->xfft)
+      if (h) cufftDestroy(h);
   job_release(j, j->traj);
   job_release(j, j->at_ind);
   job_release(j, j->fine);
@@ -1303,9 +1310,59 @@ extern "C" int mpsq_job_estimate_bytes(const mpsq_job_desc* d, int64_t* bytes) {
     b += (int64_t)std::max(1, ng) * g.n_fine * 8 + (int64_t)(std::max(1, ng) * g.n_tiles + 1) * 8 +
          d->n_atoms_frame * per * (int64_t)(rsize(d->precision) + csize(d->precision)) + b1 + prep;
   } else {
-    b += g.n_fine * (int64_t)csize(d->precision) / 4;  // cuFFT work area (estimate)
+    // cuFFT work areas (estimate): the strided (z, y) plans of the kept x columns of a 3D grid
+    // hold up to their own data each, about a quarter of the grid per plan
+    b += g.n_fine * (int64_t)csize(d->precision) / (d->ndim == 3 ? 2 : 4);
   }
   *bytes = b;
+  return MPSQ_OK;
+}
+
+// Volumes on cuFFT (FP64, and FP32 fine grids off the compiled length ladder) transform only
+// what the deconvolution reads: one batch of x transforms over every row, then batched 2D
+// (z, y) transforms over the x columns whose frequencies are kept, [0, h0] and [n0 - h0, n0)
+// with h0 = m0 / 2 (the modes and their mirrors), strided by n0 within each grid.  About half
+// the columns take the (z, y) part, so the transform does ~2/3 of a full 3D one.
+static int make_xpruned_fft(mpsq_job* j) {
+  const GridGeom& g = j->g;
+  const cufftType type = j->d.precision == MPSQ_FP64 ? CUFFT_Z2Z : CUFFT_C2C;
+  const long long n0 = g.nf[0], n1 = g.nf[1], n2 = g.nf[2];
+  const int h0 = (int)(g.m[0] / 2);
+  long long nx[1] = {n0};
+  long long nzy[2] = {n2, n1};
+  const long long batch[3] = {(long long)j->sa.ngrid * n1 * n2, h0 + 1, h0};
+  for (int k = 0; k < 3; ++k) {
+    if (batch[k] == 0) continue;
+    MPSQ_CUFFT_TRY(cufftCreate(&j->xfft[k]));
+    j->have_xfft = true;
+    size_t ws = 0;
+    cufftResult r = k == 0 ? cufftMakePlanMany64(j->xfft[k], 1, nx, nullptr, 1, n0, nullptr, 1, n0,
+                                                 type, batch[k], &ws)
+                           : cufftMakePlanMany64(j->xfft[k], 2, nzy, nzy, n0, 1, nzy, n0, 1, type,
+                                                 batch[k], &ws);
+    if (r == CUFFT_SUCCESS) r = cufftSetStream(j->xfft[k], j->s);
+    if (r != CUFFT_SUCCESS)
+      return fail(MPSQ_ERR_CUFFT, "cufftMakePlanMany (%s part, %lld x %lld x %lld) status %d",
+                  k == 0 ? "x" : "z-y", n0, n1, n2, (int)r);
+  }
+  j->xfft_h0 = h0;
+  return MPSQ_OK;
+}
+
+static int exec_xpruned_fft(mpsq_job* j) {
+  const int prec = j->d.precision;
+  const size_t cs = prec == MPSQ_FP64 ? sizeof(double2) : sizeof(float2);
+  char* base = static_cast<char*>(j->fine);
+  int rc = exec_fft(j->xfft[0], prec, base, CUFFT_FORWARD);
+  if (rc) return rc;
+  const int64_t n0 = j->g.nf[0];
+  for (int gi = 0; gi < j->sa.ngrid; ++gi) {
+    char* grid = base + (size_t)gi * j->g.n_fine * cs;
+    rc = exec_fft(j->xfft[1], prec, grid, CUFFT_FORWARD);
+    if (!rc && j->xfft[2])
+      rc = exec_fft(j->xfft[2], prec, grid + (size_t)(n0 - j->xfft_h0) * cs, CUFFT_FORWARD);
+    if (rc) return rc;
+  }
   return MPSQ_OK;
 }
 
@@ -1552,12 +1609,20 @@ extern "C" int mpsq_job_create(const mpsq_job_desc* d, void* stream, mpsq_job** 
       }
     }
   } else {
-    rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
-    if (rc) {
-      job_free(j);
-      return rc;
+    if (d->ndim == 3) {
+      rc = make_xpruned_fft(j);
+      if (rc) {
+        job_free(j);
+        return rc;
+      }
+    } else {
+      rc = make_fft_plan(j->g, a.ngrid, prec, j->s, &j->fft);
+      if (rc) {
+        job_free(j);
+        return rc;
+      }
+      j->have_fft = true;
     }
-    j->have_fft = true;
   }
   *out = j;
   return MPSQ_OK;
@@ -1776,7 +1841,8 @@ static int job_transform_body(mpsq_job* j, int32_t first, int32_t count) {
       }
     }
     if (!done) {
-      rc = exec_fft(j->fft, j->d.precision, j->fine, CUFFT_FORWARD);
+      rc = j->have_xfft ? exec_xpruned_fft(j) : exec_fft(j->fft, j->d.precision, j->fine,
+                                                          CUFFT_FORWARD);
       if (rc) return rc;
       if (mark(3)) return MPSQ_ERR_CUDA;
       const dim3 dgrid((unsigned)((j->g.m[0] + 127) / 128), (unsigned)j->g.m[1],
