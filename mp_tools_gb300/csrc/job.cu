@@ -775,9 +775,14 @@ __global__ void __launch_bounds__(16 * L, (N < 512 ? 48 / L : 1))
   for (int p = 0; p < LOADS; ++p) {
     const int e = tid + NT * p;
     if (e < LP * NP) {
-      const int rp = e % LP, x = 2 * (e / LP);
-      *reinterpret_cast<float4*>(&xs[x * L + 2 * rp]) = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
-      *reinterpret_cast<float4*>(&xs[(x + 1) * L + 2 * rp]) = make_float4(va[p].z, va[p].w, vb[p].z, vb[p].w);
+      const int rp = e % LP, xp = e / LP, x = 2 * xp;
+      const float4 lo = make_float4(va[p].x, va[p].y, vb[p].x, vb[p].y);
+      const float4 hi = make_float4(va[p].z, va[p].w, vb[p].z, vb[p].w);
+      // 8-line rows are 64 bytes: lanes of odd xp store their second row first, so that each
+      // store instruction of a warp covers both halves of the banks (4 wavefronts, not 8)
+      const int odd = L == 8 ? (xp & 1) : 0;
+      *reinterpret_cast<float4*>(&xs[(x + odd) * L + 2 * rp]) = odd ? hi : lo;
+      *reinterpret_cast<float4*>(&xs[(x + 1 - odd) * L + 2 * rp]) = odd ? lo : hi;
     }
   }
   __syncthreads();
