@@ -13,7 +13,9 @@
 // accumulators).  FP32 accuracy is kept by splitting each operand v into two f16 terms:
 // hi = v with its 13 low mantissa bits cleared (exact in f16), lo = v - hi (exact in FP32,
 // rounded to f16), and accumulating Ah*Bh + Ah*Bl + Al*Bh; the dropped Al*Bl term and the
-// rounding of lo are below 2^-21 of each product.  A and B carry a factor 2^10 so that the lo
+// rounding of lo are below 2^-21 of each product.  From width 8 on (tolerances near 1e-7) the
+// Al*Bl term is accumulated too (one more MMA per product term set, ~20 % less error at ~1.3 %
+// more step time).  A and B carry a factor 2^10 so that the lo
 // terms of kernel values down to ~1e-4 stay in the f16 normal range; the tile is scaled by
 // 2^-20 when it is written.  Strengths must satisfy |s| <= 8 (the spatial Hann window's
 // maximum), which keeps |A| <= 2^13 well inside the f16 range.
@@ -225,6 +227,13 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
       uint32_t ah0[4], al0[4], ah1[4], al1[4];
       build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah0, al0);
       build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah1, al1);
+      if constexpr (W >= 8) {
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          mma_16816(acc[0][nt], al0, bl[nt][0], bl[nt][1]);
+          mma_16816(acc[1][nt], al1, bl[nt][0], bl[nt][1]);
+        }
+      }
 #pragma unroll
       for (int nt = 0; nt < 2; ++nt) {
         mma_16816(acc[0][nt], al0, bh[nt][0], bh[nt][1]);
@@ -243,6 +252,10 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
     } else if (use0) {
       uint32_t ah[4], al[4];
       build_a(sm, p0, first, t, yA0, yA1, yB0, yB1, ah, al);
+      if constexpr (W >= 8) {
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) mma_16816(acc[0][nt], al, bl[nt][0], bl[nt][1]);
+      }
 #pragma unroll
       for (int nt = 0; nt < 2; ++nt) mma_16816(acc[0][nt], al, bh[nt][0], bh[nt][1]);
 #pragma unroll
@@ -252,6 +265,10 @@ __device__ __forceinline__ void mma_region(const MmaSmem<W>& sm, int kb0, int kb
     } else {
       uint32_t ah[4], al[4];
       build_a(sm, p0 + 1, first, t, yA0, yA1, yB0, yB1, ah, al);
+      if constexpr (W >= 8) {
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) mma_16816(acc[1][nt], al, bl[nt][0], bl[nt][1]);
+      }
 #pragma unroll
       for (int nt = 0; nt < 2; ++nt) mma_16816(acc[1][nt], al, bh[nt][0], bh[nt][1]);
 #pragma unroll
