@@ -12,6 +12,10 @@ module mpsq_api
   integer(c_int), parameter, public :: MPSQ_CELL = 0, MPSQ_BULK = 1
   integer(c_int), parameter, public :: MPSQ_WEIGHT_UNIT = 1, MPSQ_WEIGHT_NEUTRON = 2, &
                                        MPSQ_WEIGHT_XRAY = 3
+  ! run-time choices (mpsq_job_set_option / mpsq_job_get_option)
+  integer(c_int), parameter, public :: MPSQ_OPT_GRAPH = 1, MPSQ_OPT_SPREAD = 2, &
+                                       MPSQ_OPT_XROWS = 3, MPSQ_OPT_LANES = 4, &
+                                       MPSQ_OPT_ZSLAB = 5, MPSQ_OPT_REPRODUCIBLE = 6
 
   type, bind(C), public :: mpsq_job_desc_t
     integer(c_int32_t) :: ndim
@@ -167,6 +171,45 @@ module mpsq_api
       integer(c_int32_t), value :: first, count, plane, n_bz
       real(c_float), value :: qx_min, qy_min
       real(c_float), intent(in) :: at_base(*)       ! at_base(3, n_species)
+    end function
+
+    integer(c_int) function mpsq_job_set_q_slab(job, z0) bind(C, name="mpsq_job_set_q_slab")
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: job
+      integer(c_int64_t), value :: z0
+    end function
+
+    integer(c_int) function mpsq_job_set_option(job, option, val) &
+        bind(C, name="mpsq_job_set_option")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: job
+      integer(c_int), value :: option, val
+    end function
+
+    integer(c_int) function mpsq_job_get_option(job, option, val) &
+        bind(C, name="mpsq_job_get_option")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: job
+      integer(c_int), value :: option
+      integer(c_int), intent(out) :: val
+    end function
+
+    integer(c_int) function mpsq_job_autotune(job, first, count, cache_path, choice, best_ms) &
+        bind(C, name="mpsq_job_autotune")
+      import :: c_int, c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: job
+      integer(c_int32_t), value :: first, count
+      type(c_ptr), value :: cache_path                ! C string (c_null_char-terminated) or null
+      integer(c_int), intent(out) :: choice(4)       ! graph, spread, xrows, lanes
+      real(c_double), intent(out) :: best_ms
+    end function
+
+    integer(c_int) function mpsq_job_info(job, width, fine_grid, n_grids, pruned, lanes) &
+        bind(C, name="mpsq_job_info")
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: job
+      integer(c_int), intent(out) :: width, n_grids, pruned, lanes
+      integer(c_int64_t), intent(out) :: fine_grid(3)
     end function
 
     type(c_ptr) function mpsq_last_error() bind(C, name="mpsq_last_error")
