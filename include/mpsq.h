@@ -317,7 +317,7 @@ int mpsq_job_set_q_slab(mpsq_job* job, int64_t z0);
  *                   1: the tensor-core spreading orders each tile's records by content first,
  *                   so that every run, schedule (graph, lanes, z-slabs, other jobs on the GPU)
  *                   and job instance gives bit-identical results (FP32 volumes with packed
- *                   pairs; about 20 % more spreading time). */
+ *                   pairs; about 20 % more spreading time, 8 % more per frame). */
 #define MPSQ_OPT_GRAPH   1
 #define MPSQ_OPT_SPREAD  2
 #define MPSQ_OPT_XROWS   3

@@ -60,6 +60,7 @@ struct MmaSmem {
   RecF rec[kCh];                         // the record sorted into each slot
   float str[kCh];                        // its real strength
   int member[kCh];                       // the chunk's records grouped by key (chunk order)
+  unsigned long long order[kCh];         // their first ordering word (cell offsets, dz bits)
   int count[2 * kKeys];
   int base[2 * kKeys];
   int tcount[2 * kKeys];                 // records per key over the whole tile (large tiles)
@@ -414,20 +415,24 @@ __global__ void __launch_bounds__(256, 3)
     //    accumulation order, follow from the record set alone; records equal in every bit may
     //    take either order
     int pos = rank;
+    const uint64_t mine =
+        tid < n ? ((uint64_t)(uint32_t)rec.packed << 32) | __float_as_uint(rec.dz) : 0ull;
     if (REPRO) {
-      if (tid < n) sm.member[sm.base[k] + rank] = tid;
+      if (tid < n) {
+        sm.member[sm.base[k] + rank] = tid;
+        sm.order[sm.base[k] + rank] = mine;
+      }
       __syncthreads();
     }
     if (REPRO && tid < n) {
       pos = 0;
-      const uint64_t mine = ((uint64_t)(uint32_t)rec.packed << 32) | __float_as_uint(rec.dz);
       const int b = sm.base[k], cnt = sm.count[k];
       for (int q = b; q < b + cnt; ++q) {
-        const int o = sm.member[q];
-        const RecF& u = sm.rec[o];
-        const uint64_t other = ((uint64_t)(uint32_t)u.packed << 32) | __float_as_uint(u.dz);
+        const uint64_t other = sm.order[q];   // one load per member; the record only on a tie
         bool before = other < mine;
-        if (other == mine && o != tid) {
+        if (other == mine && q != b + rank) {
+          const int o = sm.member[q];
+          const RecF& u = sm.rec[o];
           const uint32_t a[3] = {__float_as_uint(u.dy), __float_as_uint(u.dx), __float_as_uint(sm.str[o])};
           const uint32_t m[3] = {__float_as_uint(rec.dy), __float_as_uint(rec.dx), __float_as_uint(sv)};
           before = a[0] != m[0] ? a[0] < m[0] : a[1] != m[1] ? a[1] < m[1] : a[2] != m[2] ? a[2] < m[2] : o < tid;
